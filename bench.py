@@ -1,0 +1,394 @@
+#!/usr/bin/env python
+"""bench.py -- in-place layout-conversion throughput on GB300.
+
+Workload (the headline of the benchmark spec): in-place 100 transposition of a
+16384 x 12289 float32 matrix, i.e. lm_transpose_100(A=16384, B=12289, b=1)
+-- 805,371,904 payload bytes; 12289 is prime, so the cycles are long and
+uneven.  One step = one full in-place transposition; steps alternate
+(A, B) = (16384, 12289) and (12289, 16384), so every second step restores the
+input, which is checked on the device at the end.
+
+Metric (the reference's own, include/cl_profile.h:43-52): GB/s = 2 x payload
+bytes / time, and its fraction of the measured HBM copy bandwidth.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Multi-GPU: the op does not shard (one matrix, one GPU); N > 1 runs N
+independent replicas under torchrun ("scaling": "weak"), max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+A0, B0, SUB, EB = 16384, 12289, 1, 4
+PAYLOAD = A0 * B0 * SUB * EB  # 805,371,904 bytes
+METRIC = "inplace_transpose_GBps"
+UNIT = "GB/s"
+CONFIG = {
+    "workload": "inplace_100_16384x12289_f32",
+    "op": "lm_transpose_100(A=16384, B=12289, b=1), elem_bytes=4, in place",
+    "payload_bytes": PAYLOAD,
+    "algorithmic_bytes_per_step": 2 * PAYLOAD,
+    "l2": "inputs larger than L2 (805 MB vs 126 MB); no flush needed",
+    "steps_alternate": "(16384,12289) then (12289,16384)",
+}
+# DRAM traffic of the dominant kernel per launch, from one ncu capture
+# (profiles/); None until captured.
+NCU_TRAFFIC = {}
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---- clocks ------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100", "-i",
+                 str(self.index)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def mark(self, which):
+        setattr(self, which, time.time())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            return None
+        rows = []
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                ts = time.mktime(time.strptime(parts[0].split(".")[0],
+                                               "%Y/%m/%d %H:%M:%S"))
+                rows.append((ts, float(parts[2]), float(parts[3]), parts[6:10]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        lo, hi = (self.t0 or 0) - 1.0, (self.t1 or 1e18) + 1.0
+        load = [r for r in rows if lo <= r[0] <= hi] or rows
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap")
+        for r in load:
+            for n, v in zip(names, r[3]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(r[1] for r in load),
+                "sm_max_mhz": max(r[2] for r in load),
+                "reasons": sorted(reasons), "samples": len(load)}
+
+
+# ---- distributed -------------------------------------------------------------
+
+def dist_setup(n):
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- CPU baseline (the reference's CPU path, restated in the oracle) ---------
+
+def cpu_transpose_rate(seconds=1.5, threads=None):
+    """GB/s of the reference's out-of-place CPU layout (cpu_soa_asta,
+    test/cl_unittest.cc:153-166, restated in oracle/lm_oracle.c) for the same
+    100(16384, 12289, 1) fp32 workload, split over `threads` host threads.
+    Runs whole transpositions until `seconds` have passed (at least one)."""
+    import numpy as np
+    from oracle import lm_oracle as O
+    threads = threads or os.cpu_count() or 1
+    src = np.empty(A0 * B0, dtype=np.uint32)
+    O.lib().lmo_fill_splitmix64(src.ctypes.data, src.nbytes, 1)
+    dst = np.empty_like(src)
+    L = O.lib()
+    # warm the pages
+    L.lmo_soa_asta_mt(src.ctypes.data, dst.ctypes.data, B0 * SUB, A0, SUB, EB,
+                      threads)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        L.lmo_soa_asta_mt(src.ctypes.data, dst.ctypes.data, B0 * SUB, A0, SUB,
+                          EB, threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return 2.0 * PAYLOAD * reps / el / 1e9, threads, reps, el
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    from oracle import lm_oracle as O
+    import numpy as np
+    threads = os.cpu_count() or 1
+    src = np.empty(A0 * B0, dtype=np.uint32)
+    O.lib().lmo_fill_splitmix64(src.ctypes.data, src.nbytes, 1)
+    dst = np.empty_like(src)
+    L = O.lib()
+
+    def step():
+        L.lmo_soa_asta_mt(src.ctypes.data, dst.ctypes.data, B0 * SUB, A0, SUB,
+                          EB, threads)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    value = 2.0 * PAYLOAD * args.steps / el / 1e9
+    sample = ("each step: one full out-of-place 100(16384,12289,1) fp32 "
+              "transposition (cpu_soa_asta loop) over %d threads" % threads)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(el / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (splitmix64 random bits)",
+        "config": CONFIG, "impl": "reference",
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT,
+                         "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---- our arm -----------------------------------------------------------------
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from libmarshal_gb300 import lm
+
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    L = lm.lib()
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234 + rank)
+    buf = torch.empty(PAYLOAD // 4, dtype=torch.int32, device=dev)
+    buf.random_(generator=g)
+    orig = buf.clone()
+    ptr = buf.data_ptr()
+    shapes = [(A0, B0), (B0, A0)]
+    count = [0]
+
+    def step():
+        A, B = shapes[count[0] & 1]
+        count[0] += 1
+        if L.lm_transpose_100(sp, ptr, EB, A, B, SUB, None):
+            raise RuntimeError("lm_transpose_100: " + lm.last_error())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local if ws > 1 else 0)
+    if rank == 0:
+        clocks.start()
+        clocks.mark("t0")
+        # untimed clock soak (~1 s of the same work) so the sampler sees load
+        t_soak = time.time()
+        while time.time() - t_soak < 1.0:
+            step()
+            step()
+            torch.cuda.synchronize()
+
+    barrier(ws)
+    torch.cuda.synchronize()
+    lm.prof_collect()  # drop anything recorded so far
+    lm.prof_enable(True)
+    launches0 = lm.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = lm.launch_count() - launches0
+    lm.prof_enable(False)
+    prof = lm.prof_collect()
+    if rank == 0:
+        clocks.mark("t1")
+        clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ws, ms)
+
+    # restore the input (even number of steps) and verify on the device
+    if count[0] & 1:
+        step()
+    torch.cuda.synchronize()
+    verified = bool(torch.equal(buf, orig))
+    del orig
+
+    value = ws * 2.0 * PAYLOAD * args.steps / (ms / 1e3) / 1e9
+    peak, peak_kind = peak_hbm()
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if dom:
+        name, (n, tot) = dom
+        per = tot / n
+        achieved = 2.0 * PAYLOAD / (per / 1e3) / 1e9
+        tr = NCU_TRAFFIC.get(name)
+        roof = {"bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": tr,
+                "kernel": name, "launches": n, "avg_ms": round(per, 4),
+                "algorithmic_bytes_per_launch": 2 * PAYLOAD,
+                "peak_kind": peak_kind,
+                "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)}
+                            for k, v in prof.items()}}
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if rank == 0 or ws > 1:
+        h_in = torch.empty(PAYLOAD, dtype=torch.uint8, pin_memory=True)
+        h_out = torch.empty(PAYLOAD, dtype=torch.uint8, pin_memory=True)
+        h_in.copy_(buf.view(torch.uint8).cpu())
+        d = torch.empty(PAYLOAD, dtype=torch.uint8, device=dev)
+
+        def e2e_step(i):
+            A, B = shapes[i & 1]
+            d.copy_(h_in, non_blocking=True)
+            if L.lm_transpose_100(sp, d.data_ptr(), EB, A, B, SUB, None):
+                raise RuntimeError(lm.last_error())
+            h_out.copy_(d, non_blocking=True)
+
+        for i in range(max(1, args.warmup)):
+            e2e_step(i)
+        torch.cuda.synchronize()
+        ke = max(3, min(args.steps, 20))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(ke):
+            e2e_step(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = e0.elapsed_time(e1) / ke
+        e2e = {"value": round(2.0 * PAYLOAD / (ems / 1e3) / 1e9, 3),
+               "unit": UNIT, "h2d_bytes_per_step": PAYLOAD,
+               "d2h_bytes_per_step": PAYLOAD, "ms_per_step": round(ems, 3)}
+        del h_in, h_out, d
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        rate, thr, reps, el = cpu_transpose_rate()
+        cpu = {"value": round(rate, 3), "unit": UNIT, "cores": thr,
+               "kind": "port",
+               "sample": "%d full out-of-place 100(16384,12289,1) fp32 "
+                         "transpositions (cpu_soa_asta loop), %.2f s" % (
+                             reps, el)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded random bits)",
+            "config": dict(CONFIG, parallelism="replicas" if ws > 1 else
+                           "single GPU", verified_round_trip=verified),
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk, "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0 if verified else 3
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        ws = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        return run_reference(args, ws, rank)
+    ws, rank, local = dist_setup(args.gpus)
+    return run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,147 @@
+/*
+ * lm_marshal.h -- C ABI of libmarshal_gb300 (liblmarshal.so).
+ *
+ * One entry per function of the reference's OpenCL interface
+ * (include/cl_marshal.h:25-50 of libmarshal, implemented in
+ * src/cl_marshal.cc) with (cl_command_queue queue, cl_mem src) replaced by
+ * (lm_stream_t stream, void *buf, int elem_bytes):
+ *   - stream: a cudaStream_t (lm_stream_t is the same type); NULL is the
+ *     legacy default stream;
+ *   - buf: device pointer to the array, converted IN PLACE;
+ *   - elem_bytes: 1, 2, 4 or 8 (the reference fixes float or double at build
+ *     time, src/cl_marshal.cc:34-43); elements are moved as raw bits.
+ * The remaining arguments keep the reference's order and meaning.
+ *
+ * Conventions (as the reference, API.wiki:12,20):
+ *   - return false on success, true on error; lm_last_error() returns the
+ *     message of the calling thread's last error;
+ *   - calls are stream ordered and asynchronous, EXCEPT: when the
+ *     elapsed-time pointer `et` is non-NULL the call waits for its own work
+ *     and adds its GPU time in nanoseconds to *et (the reference's
+ *     Profiling::Report, include/cl_profile.h:23-25), and padding/unpadding
+ *     always wait in order to read their status word;
+ *   - scratch (done bits) comes from the device's stream-ordered memory
+ *     pool on the caller's stream; calls on different streams never share it.
+ *
+ * Notation: 010  [A][a][B]     -> [A][B][a]
+ *           100  [A][B][b]     -> [B][A][b]
+ *           0100 [A][a][B][b]  -> [A][B][a][b]
+ */
+#ifndef LIBMARSHAL_GB300_LM_MARSHAL_H_
+#define LIBMARSHAL_GB300_LM_MARSHAL_H_
+
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct CUstream_st;
+typedef struct CUstream_st *lm_stream_t; /* == cudaStream_t */
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *lm_last_error(void);
+const char *lm_version(void);
+
+/* Releases pooled scratch memory.  Reference: cl_marshal_finalize
+ * (src/cl_marshal.cc:116-119; declared by the reference's tests,
+ * test/cl_unittest.cc:99).  Both names are exported. */
+void lm_marshal_finalize(void);
+void cl_marshal_finalize(void);
+
+/* AoS [height][width] -> ASTA [height/tile][width][tile] (010).
+ * Reference: cl_aos_asta_bs, cl_marshal.h:26-27 / cl_marshal.cc:793-800. */
+bool lm_aos_asta_bs(lm_stream_t stream, void *buf, int elem_bytes, int height,
+                    int width, int tile_size);
+/* Reference: cl_aos_asta_pttwac, cl_marshal.h:28-29 / cl_marshal.cc:803-812.
+ * R: spreading factor of the done-bit map (power of two, 1..32); P: padding
+ * words per 32 flag words. */
+bool lm_aos_asta_pttwac(lm_stream_t stream, void *buf, int elem_bytes,
+                        int height, int width, int tile_size, int R, int P);
+/* BS first, PTTWAC only if BS failed; true only if both failed.
+ * Reference: cl_aos_asta, cl_marshal.h:30-31 / cl_marshal.cc:814-818. */
+bool lm_aos_asta(lm_stream_t stream, void *buf, int elem_bytes, int height,
+                 int width, int tile_size, int R);
+
+/* Full in-place transposition [A*a][B*b] -> [B*b][A*a] through the staged
+ * elementary transpositions; stages = 2, 22, 3, 32 or 4, anything else the
+ * element-wise fallback.  et may be NULL.
+ * Reference: cl_transpose, cl_marshal.h:32-33 / cl_marshal.cc:561-776. */
+bool lm_transpose(lm_stream_t stream, void *buf, int elem_bytes, int A, int a,
+                  int B, int b, int R, int stages, unsigned long long *et);
+/* Same with the variant of every 010 step forced: 0 = as lm_transpose (BS when
+ * the tile fits on chip, else PTTWAC), 1 = BS, 2 = PTTWAC.  No reference
+ * counterpart (the reference picks by MAX_MEM, cl_marshal.cc:578-585). */
+bool lm_transpose_ex(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                     int a, int B, int b, int R, int stages, int variant010,
+                     unsigned long long *et);
+
+/* 010 by barrier-synchronised tiles.  Reference: cl_transpose_010_bs,
+ * cl_marshal.h:35-36 / cl_marshal.cc:136-277.  Returns true when the tile
+ * exceeds on-chip capacity (the reference fails the same way past MAX_MEM). */
+bool lm_transpose_010_bs(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                         int a, int B, unsigned long long *et);
+/* 010 by in-tile cycle following.  Reference: cl_transpose_010_pttwac,
+ * cl_marshal.h:37-38 / cl_marshal.cc:280-336. */
+bool lm_transpose_010_pttwac(lm_stream_t stream, void *buf, int elem_bytes,
+                             int A, int a, int B, unsigned long long *et,
+                             int R, int P);
+/* 100 [A][B][b] -> [B][A][b].  Reference: cl_transpose_100,
+ * cl_marshal.h:40-41 / cl_marshal.cc:779-782. */
+bool lm_transpose_100(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                      int B, int b, unsigned long long *et);
+/* 0100 [A][a][B][b] -> [A][B][a][b].  Reference: cl_transpose_0100,
+ * cl_marshal.h:43-44 / cl_marshal.cc:785-788. */
+bool lm_transpose_0100(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                       int a, int B, int b, unsigned long long *et);
+/* 0100 with the algorithm forced: 0 = planner, 1 = BS (on-chip tiles),
+ * 2 = PTTWAC on b-element units.  No reference counterpart (the reference
+ * picks by super-element size, cl_marshal.cc:365-370). */
+bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
+                              int A, int a, int B, int b, int method,
+                              unsigned long long *et);
+
+/* Row padding [y_size][x_size] -> [y_size][pad_size] (new columns zero) and
+ * unpadding [y_size][pad_size] -> [y_size][x_size] (tail zero).  buf holds
+ * y_size*pad_size elements.  Reference: cl_padding / cl_unpadding,
+ * cl_marshal.h:46-49 / cl_marshal.cc:821-956. */
+bool lm_padding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
+                int y_size, int pad_size, unsigned long long *et);
+bool lm_unpadding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
+                  int y_size, int pad_size, unsigned long long *et);
+
+/* 1 when a 0100 tile [a][B][b] (T tiles) of elem_bytes elements can be staged
+ * on chip (shared memory of one CTA or of a thread-block cluster), else 0.
+ * Counterpart of T010_BS::IsFeasible (include/plan.hpp:108-111). */
+int lm_bs_feasible(long long T, int a, int B, int b, int elem_bytes);
+
+/* Failure-detection hook (no reference counterpart): padding (unpad == 0) or
+ * unpadding whose task `stall_block` waits on a flag nothing sets.  The wait
+ * gives up after timeout_ns; the call must return true and leave the CUDA
+ * context usable. */
+bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
+                        int x_size, int y_size, int pad_size, int unpad,
+                        long long stall_block, unsigned long long timeout_ns);
+
+/* ---- profiling (counterpart of include/cl_profile.h:6-63) ----------------
+ * lm_launch_count: kernels launched by this library since it was loaded.
+ * lm_prof_enable(1): from now on every launch is bracketed by a CUDA event
+ * pair on its stream.  lm_prof_collect: waits for the recorded events, writes
+ * up to cap per-kernel entries (launches, summed device ms), clears the
+ * record, and returns the number of distinct kernels. */
+typedef struct {
+  char name[48];
+  long long launches;
+  double total_ms;
+} lm_prof_entry;
+unsigned long long lm_launch_count(void);
+void lm_prof_enable(int on);
+int lm_prof_collect(lm_prof_entry *out, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBMARSHAL_GB300_LM_MARSHAL_H_ */

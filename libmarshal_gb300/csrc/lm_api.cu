@@ -1,0 +1,509 @@
+// lm_api.cu -- host dispatch, planner and the exported C ABI.
+//
+// Drop-in surface (see include/marshal.h and include/lm_marshal.h):
+//   gpu_aos_asta_bs_float/double, gpu_aos_asta_pttwac, gpu_soa_asta_pttwac
+//       -- include/marshal.h:26-31 of the reference, same signatures;
+//   lm_* -- one entry per cl_* function of include/cl_marshal.h:26-49 with
+//       (cl_command_queue, cl_mem) replaced by (cudaStream_t, void *buf, int
+//       elem_bytes); same argument order, same meaning, same error convention:
+//       false on success, true on error (API.wiki:12,20), with the message
+//       available from lm_last_error().
+//
+// Everything is stream ordered.  Scratch (done bits, ticket words) comes from
+// the device's stream-ordered memory pool (cudaMallocAsync / cudaFreeAsync on
+// the caller's stream), so concurrent calls on different streams never share
+// it and repeated calls reuse pooled memory instead of allocating.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "lm_core.cuh"
+#include "lm_internal.h"
+#include "../../include/lm_marshal.h"
+#include "../../include/marshal.h"
+
+namespace lm {
+
+// ---- device info ------------------------------------------------------------
+
+const DeviceInfo &device_info() {
+  static DeviceInfo cache[64];
+  static std::mutex mu;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  DeviceInfo &d = cache[dev & 63];
+  if (d.device != dev) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (d.device != dev) {
+      DeviceInfo n;
+      n.device = dev;
+      cudaDeviceGetAttribute(&n.sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&n.max_smem_optin,
+                             cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      cudaDeviceGetAttribute(&n.max_smem_per_sm,
+                             cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+      cudaDeviceGetAttribute(&n.cc_major, cudaDevAttrComputeCapabilityMajor, dev);
+      cudaDeviceGetAttribute(&n.cc_minor, cudaDevAttrComputeCapabilityMinor, dev);
+      if (n.sms <= 0) n.sms = 1;
+      if (n.max_smem_optin <= 0) n.max_smem_optin = 48 * 1024;
+      d = n;
+    }
+  }
+  return d;
+}
+
+// ---- errors -----------------------------------------------------------------
+
+static thread_local std::string g_err;
+
+static bool fail(const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  if (getenv("LM_VERBOSE")) fprintf(stderr, "libmarshal_gb300: %s\n", buf);
+  return true;
+}
+
+static bool cuda_fail(cudaError_t e, const char *what) {
+  return fail("%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---- scratch ----------------------------------------------------------------
+
+static void pool_keep_memory() {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (done[dev & 63]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;  // keep freed blocks pooled between calls
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev & 63] = true;
+}
+
+struct Scratch {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  ~Scratch() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+static bool get_zeroed(Scratch &sc, size_t bytes, cudaStream_t s) {
+  pool_keep_memory();
+  sc.s = s;
+  cudaError_t e = cudaMallocAsync(&sc.p, bytes ? bytes : 4, s);
+  if (e != cudaSuccess) {
+    sc.p = nullptr;
+    return cuda_fail(e, "scratch allocation");
+  }
+  e = cudaMemsetAsync(sc.p, 0, bytes ? bytes : 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "scratch clear");
+  return false;
+}
+
+// ---- timing (the reference's elapsed_time accumulator) ----------------------
+
+struct OpTimer {
+  unsigned long long *et;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  OpTimer(unsigned long long *et_, cudaStream_t s_) : et(et_), s(s_) {
+    if (et) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+  }
+  // Adds the elapsed kernel time in ns (blocks, like Profiling::Report).
+  bool finish() {
+    if (!et) return false;
+    cudaEventRecord(b, s);
+    cudaError_t e = cudaEventSynchronize(b);
+    if (e != cudaSuccess) return cuda_fail(e, "timing");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    *et += (unsigned long long)((double)ms * 1.0e6);
+    return false;
+  }
+  ~OpTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+static bool valid_e(int e) { return e == 1 || e == 2 || e == 4 || e == 8; }
+
+// ---- planner ----------------------------------------------------------------
+
+enum class Method { Auto, BS, Pttwac };
+
+static bool check_launch(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return false;
+}
+
+static bool run_pttwac_direct(cudaStream_t s, void *buf, int e, uint64_t T,
+                              uint64_t a, uint64_t B, uint64_t b) {
+  const size_t fb = pttwac_flag_bytes(buf, T, (uint32_t)a, (uint32_t)B,
+                                      (uint32_t)b, e);
+  if (fb == 0) return fail("PTTWAC: shape exceeds 2^32 units per instance");
+  Scratch flags;
+  if (get_zeroed(flags, fb, s)) return true;
+  return check_launch(launch_pttwac0100(s, buf, e, T, (uint32_t)a,
+                                        (uint32_t)B, (uint32_t)b,
+                                        (uint32_t *)flags.p),
+                      "PTTWAC launch");
+}
+
+// Largest-unit-first search for a two-pass split of one 100(a, B, b):
+// returns a2 | a with a2*U in [128, 1024] bytes whose tile a2 x B x b fits BS.
+static uint64_t split_a(uint64_t a, uint64_t B, uint64_t b, int e) {
+  const uint64_t U = b * e;
+  uint64_t best = 0;
+  for (uint64_t d = 2; d <= a && d * U <= 1024; ++d) {
+    if (a % d) continue;
+    if (d * U < 128) continue;
+    BsPlan p = plan_bs0100(1, (uint32_t)d, (uint32_t)B, (uint32_t)b, e);
+    if (!p.feasible) continue;
+    best = d;
+    break;  // smallest d with a >= 128-byte unit
+  }
+  return best;
+}
+
+static uint64_t split_B(uint64_t a, uint64_t B, uint64_t b, int e) {
+  const uint64_t U = b * e;
+  for (uint64_t c = 2; c <= B && c * U <= 1024; ++c) {
+    if (B % c) continue;
+    if (c * U < 128) continue;
+    BsPlan p = plan_bs0100(1, (uint32_t)a, (uint32_t)c, (uint32_t)b, e);
+    if (!p.feasible) continue;
+    return c;
+  }
+  return 0;
+}
+
+// 0100(T, a, B, b): [T][a][B][b] -> [T][B][a][b] with e-byte elements.
+static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
+                    uint64_t B, uint64_t b, Method m) {
+  if (!valid_e(e)) return fail("element size must be 1, 2, 4 or 8 (got %d)", e);
+  if (T == 0 || a == 0 || B == 0 || b == 0) return false;  // empty
+  if (a == 1 || B == 1) return false;                      // identity
+  if (buf == nullptr) return fail("null buffer");
+  if (a * B >= 0xffffffffull) return fail("a*B must be < 2^32");
+  if (m != Method::Pttwac) {
+    BsPlan p = plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e);
+    if (p.feasible)
+      return check_launch(launch_bs0100(s, buf, e, T, (uint32_t)a,
+                                        (uint32_t)B, (uint32_t)b, p),
+                          "BS launch");
+    if (m == Method::BS)
+      return fail("BS: tile of %llu bytes exceeds on-chip capacity",
+                  (unsigned long long)(a * B * b * e));
+  }
+  const uint64_t U = b * e;
+  if (m == Method::Auto && U < 128) {
+    // Aggregate small super-elements into >=128-byte units first so the
+    // cycle-following pass moves whole cache lines.
+    uint64_t a2 = split_a(a, B, b, e);
+    if (a2) {
+      const uint64_t a1 = a / a2;
+      if (do_0100(s, buf, e, T * a1, a2, B, b, Method::BS)) return true;
+      return do_0100(s, buf, e, T, a1, B, a2 * b, Method::Auto);
+    }
+    uint64_t c = split_B(a, B, b, e);
+    if (c) {
+      const uint64_t B1 = B / c;
+      if (do_0100(s, buf, e, T, a, B1, c * b, Method::Auto)) return true;
+      return do_0100(s, buf, e, T * B1, a, c, b, Method::BS);
+    }
+  }
+  return run_pttwac_direct(s, buf, e, T, a, B, b);
+}
+
+static bool do_010_pttwac(cudaStream_t s, void *buf, int e, uint64_t A,
+                          uint64_t a, uint64_t B, int R, int P) {
+  if (!valid_e(e)) return fail("element size must be 1, 2, 4 or 8 (got %d)", e);
+  if (A == 0 || a <= 1 || B <= 1) return false;
+  if (buf == nullptr) return fail("null buffer");
+  if (R < 1 || R > 32 || (R & (R - 1))) return fail("R must be a power of two in [1, 32]");
+  if (P < 0) return fail("P must be >= 0");
+  if (a * B < 0xffffffffull && pttwac010_smem_fits((uint32_t)a, (uint32_t)B, R, P))
+    return check_launch(launch_pttwac010_smem(s, buf, e, A, (uint32_t)a,
+                                              (uint32_t)B, R, P),
+                        "010 PTTWAC launch");
+  // tile larger than the shared-memory done-bit map: done bits in HBM
+  return do_0100(s, buf, e, A, a, B, 1, Method::Pttwac);
+}
+
+static bool do_pad(cudaStream_t s, void *buf, int e, int64_t x, int64_t y,
+                   int64_t pad, bool padding, uint64_t timeout_ns,
+                   int64_t stall_block) {
+  if (!valid_e(e)) return fail("element size must be 1, 2, 4 or 8 (got %d)", e);
+  if (x < 0 || y < 0 || pad < x) return fail("padding needs 0 <= x <= pad, y >= 0");
+  if ((y == 0 || pad == x) && stall_block < 0) return false;
+  if (buf == nullptr) return fail("null buffer");
+  Scratch sc, st;
+  if (get_zeroed(sc, pad_scratch_bytes(x, y, pad), s)) return true;
+  if (get_zeroed(st, 4, s)) return true;
+  cudaError_t err =
+      padding ? launch_padding(s, buf, e, x, y, pad, (uint32_t *)sc.p,
+                               (uint32_t *)st.p, timeout_ns, stall_block)
+              : launch_unpadding(s, buf, e, x, y, pad, (uint32_t *)sc.p,
+                                 (uint32_t *)st.p, timeout_ns, stall_block);
+  if (err != cudaSuccess) return cuda_fail(err, padding ? "padding" : "unpadding");
+  uint32_t status = 0;
+  err = cudaMemcpyAsync(&status, st.p, 4, cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) return cuda_fail(err, "padding status");
+  if (status != kStatusOk)
+    return fail("%s: an inter-CTA wait timed out (status %u)",
+                padding ? "padding" : "unpadding", status);
+  return false;
+}
+
+// Staged full transposition [A*a][B*b] -> [B*b][A*a] (src/cl_marshal.cc:561-776).
+static bool do_transpose(cudaStream_t s, void *buf, int e, int64_t A,
+                         int64_t a, int64_t B, int64_t b, int R, int stages,
+                         int variant010) {
+  if (!valid_e(e)) return fail("element size must be 1, 2, 4 or 8 (got %d)", e);
+  if (A <= 0 || a <= 0 || B <= 0 || b <= 0) return fail("dimensions must be positive");
+  auto t010 = [&](int64_t AA, int64_t aa, int64_t BB) -> bool {
+    if (variant010 == 2) return do_010_pttwac(s, buf, e, AA, aa, BB, R, 1);
+    Method m = variant010 == 1 ? Method::BS : Method::Auto;
+    BsPlan p = plan_bs0100(AA, (uint32_t)aa, (uint32_t)BB, 1, e);
+    if (!p.feasible && variant010 == 0)
+      return do_010_pttwac(s, buf, e, AA, aa, BB, R, 1);
+    return do_0100(s, buf, e, AA, aa, BB, 1, m);
+  };
+  auto t100 = [&](int64_t AA, int64_t BB, int64_t bb) {
+    return do_0100(s, buf, e, 1, AA, BB, bb, Method::Auto);
+  };
+  auto t0100 = [&](int64_t AA, int64_t aa, int64_t BB, int64_t bb) {
+    return do_0100(s, buf, e, AA, aa, BB, bb, Method::Auto);
+  };
+  switch (stages) {
+    case 2:  // 010(A, a, B*b) -> 100(A, B*b, a)            (:569-601)
+      if (a > 1 && t010(A, a, B * b)) return true;
+      return t100(A, B * b, a);
+    case 22:  // 100(A*a, B, b) -> 010(B, A*a, b)           (:602-634)
+      if (t100(A * a, B, b)) return true;
+      return b > 1 ? t010(B, A * a, b) : false;
+    case 3:  // 100(A*a,B,b) -> 010(B*A,a,b) -> 0100(B,A,b,a) (:636-677)
+      if (t100(A * a, B, b)) return true;
+      if (a > 1 && t010(B * A, a, b)) return true;
+      return t0100(B, A, b, a);
+    case 32:  // 0100(A,a,B,b) -> 010(A*B,a,b) -> 100(A,B*b,a) (:679-720)
+      if (t0100(A, a, B, b)) return true;
+      if (a > 1 && t010(A * B, a, b)) return true;
+      return t100(A, B * b, a);
+    case 4:  // 0100 -> 010 -> 100(A,B,b*a) -> 0100(B,A,b,a)  (:722-767)
+      if (t0100(A, a, B, b)) return true;
+      if (t010(B * A, a, b)) return true;
+      if (t100(A, B, b * a)) return true;
+      return t0100(B, A, b, a);
+    default:  // element-wise fallback 0100(1, A*a, B*b, 1)  (:769-775)
+      return t0100(1, A * a, B * b, 1);
+  }
+}
+
+}  // namespace lm
+
+using namespace lm;
+
+// ============================================================================
+// C ABI
+// ============================================================================
+
+extern "C" {
+
+const char *lm_last_error(void) { return g_err.c_str(); }
+
+const char *lm_version(void) { return "libmarshal_gb300 1.0 (sm_103a)"; }
+
+void lm_marshal_finalize(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+    cudaMemPoolTrimTo(pool, 0);
+}
+
+// reference: cl_marshal_finalize (src/cl_marshal.cc:116-119)
+void cl_marshal_finalize(void) { lm_marshal_finalize(); }
+
+bool lm_transpose_010_bs(lm_stream_t stream, void *buf, int elem_bytes,
+                         int A, int a, int B, unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (A < 0 || a < 0 || B < 0) return fail("dimensions must be >= 0");
+  if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
+              (uint64_t)B, 1, Method::BS))
+    return true;
+  return t.finish();
+}
+
+bool lm_transpose_010_pttwac(lm_stream_t stream, void *buf, int elem_bytes,
+                             int A, int a, int B, unsigned long long *et,
+                             int R, int P) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (A < 0 || a < 0 || B < 0) return fail("dimensions must be >= 0");
+  if (do_010_pttwac((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A,
+                    (uint64_t)a, (uint64_t)B, R, P))
+    return true;
+  return t.finish();
+}
+
+bool lm_transpose_100(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                      int B, int b, unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (A < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
+  if (do_0100((cudaStream_t)stream, buf, elem_bytes, 1, (uint64_t)A,
+              (uint64_t)B, (uint64_t)b, Method::Auto))
+    return true;
+  return t.finish();
+}
+
+bool lm_transpose_0100(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                       int a, int B, int b, unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (A < 0 || a < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
+  if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
+              (uint64_t)B, (uint64_t)b, Method::Auto))
+    return true;
+  return t.finish();
+}
+
+bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
+                              int A, int a, int B, int b, int method,
+                              unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (A < 0 || a < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
+  Method m = method == 1 ? Method::BS : method == 2 ? Method::Pttwac : Method::Auto;
+  if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
+              (uint64_t)B, (uint64_t)b, m))
+    return true;
+  return t.finish();
+}
+
+bool lm_transpose(lm_stream_t stream, void *buf, int elem_bytes, int A, int a,
+                  int B, int b, int R, int stages, unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (do_transpose((cudaStream_t)stream, buf, elem_bytes, A, a, B, b, R,
+                   stages, 0))
+    return true;
+  return t.finish();
+}
+
+bool lm_transpose_ex(lm_stream_t stream, void *buf, int elem_bytes, int A,
+                     int a, int B, int b, int R, int stages, int variant010,
+                     unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (variant010 < 0 || variant010 > 2) return fail("variant010 must be 0, 1 or 2");
+  if (do_transpose((cudaStream_t)stream, buf, elem_bytes, A, a, B, b, R,
+                   stages, variant010))
+    return true;
+  return t.finish();
+}
+
+bool lm_aos_asta_bs(lm_stream_t stream, void *buf, int elem_bytes, int height,
+                    int width, int tile_size) {
+  if (tile_size <= 0 || height < 0 || width < 0 || height % tile_size)
+    return fail("height must be a multiple of tile_size");
+  return lm_transpose_010_bs(stream, buf, elem_bytes, height / tile_size,
+                             tile_size, width, nullptr);
+}
+
+bool lm_aos_asta_pttwac(lm_stream_t stream, void *buf, int elem_bytes,
+                        int height, int width, int tile_size, int R, int P) {
+  if (tile_size <= 0 || height < 0 || width < 0 || height % tile_size)
+    return fail("height must be a multiple of tile_size");
+  return lm_transpose_010_pttwac(stream, buf, elem_bytes, height / tile_size,
+                                 tile_size, width, nullptr, R, P);
+}
+
+bool lm_aos_asta(lm_stream_t stream, void *buf, int elem_bytes, int height,
+                 int width, int tile_size, int R) {
+  // src/cl_marshal.cc:814-818: BS, and PTTWAC only if BS reported an error.
+  return lm_aos_asta_bs(stream, buf, elem_bytes, height, width, tile_size) &&
+         lm_aos_asta_pttwac(stream, buf, elem_bytes, height, width, tile_size,
+                            R, 1);
+}
+
+bool lm_padding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
+                int y_size, int pad_size, unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (do_pad((cudaStream_t)stream, buf, elem_bytes, x_size, y_size, pad_size,
+             true, 2000000000ull, -1))
+    return true;
+  return t.finish();
+}
+
+bool lm_unpadding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
+                  int y_size, int pad_size, unsigned long long *et) {
+  OpTimer t(et, (cudaStream_t)stream);
+  if (do_pad((cudaStream_t)stream, buf, elem_bytes, x_size, y_size, pad_size,
+             false, 2000000000ull, -1))
+    return true;
+  return t.finish();
+}
+
+// Failure-detection hook: runs padding (or unpadding) with task `stall_block`
+// waiting on a flag that is never set, bounded by timeout_ns.  Must return
+// true (error) with a timeout message and leave the context usable.
+bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
+                        int x_size, int y_size, int pad_size, int unpad,
+                        long long stall_block, unsigned long long timeout_ns) {
+  return do_pad((cudaStream_t)stream, buf, elem_bytes, x_size, y_size,
+                pad_size, unpad == 0, timeout_ns, stall_block);
+}
+
+// Planner query used by the Python API's IsFeasible(): 1 when the 0100 tile
+// [a][B][b] of elem_bytes elements can be staged on chip (BS), else 0.
+int lm_bs_feasible(long long T, int a, int B, int b, int elem_bytes) {
+  if (!valid_e(elem_bytes) || T <= 0 || a <= 0 || B <= 0 || b <= 0) return 0;
+  return plan_bs0100((uint64_t)T, (uint32_t)a, (uint32_t)B, (uint32_t)b,
+                     elem_bytes).feasible ? 1 : 0;
+}
+
+// ---- reference CUDA drop-ins (include/marshal.h:26-31) ----------------------
+// Same signatures; launch on the legacy default stream like the reference
+// (src/marshal.cu:27-80).  `timer` is accepted and left untouched, as the
+// reference kernels never write it.
+
+bool gpu_aos_asta_bs_float(float *src, int height, int width, int tile_size,
+                           clock_t *timer) {
+  (void)timer;
+  return lm_aos_asta_bs(nullptr, src, 4, height, width, tile_size);
+}
+
+bool gpu_aos_asta_bs_double(double *src, int height, int width, int tile_size,
+                            clock_t *timer) {
+  (void)timer;
+  return lm_aos_asta_bs(nullptr, src, 8, height, width, tile_size);
+}
+
+bool gpu_aos_asta_pttwac(float *src, int height, int width, int tile_size,
+                         clock_t *timer) {
+  (void)timer;
+  return lm_aos_asta_pttwac(nullptr, src, 4, height, width, tile_size, 1, 0);
+}
+
+bool gpu_soa_asta_pttwac(float *src, int height, int width, int tile_size,
+                         clock_t *timer) {
+  (void)timer;
+  // [w][h/t][t] -> [h/t][w][t] == 100(A=w, B=h/t, b=t)
+  if (tile_size <= 0 || height < 0 || width < 0 || height % tile_size)
+    return fail("height must be a multiple of tile_size");
+  return lm_transpose_100(nullptr, src, 4, width, height / tile_size,
+                          tile_size, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+// lm_internal.h -- interface between the host dispatch (lm_api.cu) and the
+// kernel launchers.  Every launcher is stream-ordered, allocates nothing
+// (scratch is passed in) and returns cudaSuccess or the launch error.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lm {
+
+struct DeviceInfo {
+  int device = -1;
+  int sms = 0;
+  int max_smem_optin = 0;   // bytes per CTA, opt-in maximum
+  int max_smem_per_sm = 0;
+  int cc_major = 0, cc_minor = 0;
+};
+const DeviceInfo &device_info();  // current device, cached
+
+// Every kernel launch of the library is wrapped in a ProfScope: it counts the
+// launch and, while profiling is on (lm_prof_enable), records a CUDA event
+// pair around it on the launching stream (lm_prof.cu).
+class ProfScope {
+ public:
+  ProfScope(cudaStream_t s, const char *name);
+  ~ProfScope();
+  ProfScope(const ProfScope &) = delete;
+  ProfScope &operator=(const ProfScope &) = delete;
+
+ private:
+  cudaStream_t s_;
+  const char *name_;
+  void *a_ = nullptr, *b_ = nullptr;
+};
+
+// ---- 0100 by barrier-synchronised tiles in shared memory ------------------
+// [T][a][B][b] -> [T][B][a][b]; elements of e bytes.  Each tile (a*B*b*e
+// bytes) is staged on chip: several tiles per CTA when small, one tile per
+// CTA, or one tile spread over a thread-block cluster (distributed shared
+// memory) when it exceeds one CTA's shared memory.
+struct BsPlan {
+  bool feasible = false;
+  int cluster = 1;             // CTAs per tile (1, 2, 4, 8 or 16)
+  uint32_t tiles_per_chunk = 1;
+  uint32_t rows_per_cta = 0;   // rows of B*b elements held by one CTA
+  uint32_t pitch = 0;          // shared-memory bytes per row
+  size_t smem_bytes = 0;       // per CTA
+  int threads = 512;
+};
+BsPlan plan_bs0100(uint64_t T, uint32_t a, uint32_t B, uint32_t b, int e,
+                   size_t smem_budget = 0 /*0: device maximum*/);
+cudaError_t launch_bs0100(cudaStream_t s, void *buf, int e, uint64_t T,
+                          uint32_t a, uint32_t B, uint32_t b,
+                          const BsPlan &plan);
+
+// ---- 0100 by cycle following with done-bits in global memory -------------
+// A instances of 100(a, B, b): units of b*e bytes; one done bit per unit.
+// `flags` must hold pttwac_flag_bytes(...) zeroed bytes.
+size_t pttwac_flag_bytes(const void *buf, uint64_t T, uint32_t a, uint32_t B,
+                         uint32_t b, int e);
+cudaError_t launch_pttwac0100(cudaStream_t s, void *buf, int e, uint64_t T,
+                              uint32_t a, uint32_t B, uint32_t b,
+                              uint32_t *flags);
+
+// ---- 010 by in-tile cycle following with done-bits in shared memory ------
+// [A][a][B] -> [A][B][a].  R is the spreading factor of the done-bit map
+// (power of two, 1..32) and P the padding words per 32 flag words.
+bool pttwac010_smem_fits(uint32_t a, uint32_t B, int R, int P);
+cudaError_t launch_pttwac010_smem(cudaStream_t s, void *buf, int e,
+                                  uint64_t A, uint32_t a, uint32_t B, int R,
+                                  int P);
+
+// ---- row padding / unpadding with bounded inter-CTA waits ----------------
+// padding:   [y][x] -> [y][pad] (new columns zero)
+// unpadding: [y][pad] -> [y][x], tail y*x..y*pad-1 zero.
+// `scratch` must hold pad_scratch_bytes(...) zeroed bytes; `status` one
+// zeroed word that the kernel sets to kStatusWaitTimeout when a wait runs
+// out.  stall_block >= 0 makes that block wait on a flag nothing sets
+// (failure-detection test hook).
+size_t pad_scratch_bytes(uint64_t x, uint64_t y, uint64_t pad);
+cudaError_t launch_padding(cudaStream_t s, void *buf, int e, uint64_t x,
+                           uint64_t y, uint64_t pad, uint32_t *scratch,
+                           uint32_t *status, uint64_t timeout_ns,
+                           int64_t stall_block);
+cudaError_t launch_unpadding(cudaStream_t s, void *buf, int e, uint64_t x,
+                             uint64_t y, uint64_t pad, uint32_t *scratch,
+                             uint32_t *status, uint64_t timeout_ns,
+                             int64_t stall_block);
+
+}  // namespace lm

@@ -1,0 +1,250 @@
+"""ctypes binding of liblmarshal.so (the C ABI declared in include/*.h).
+
+Buffers are PyTorch CUDA tensors (any dtype; the element width is the
+tensor's element size unless ``elem_bytes`` is given) or raw device pointers
+(ints, with ``elem_bytes`` required).  Streams are ``torch.cuda.Stream``,
+raw ``cudaStream_t`` ints, or None for torch's current stream.
+
+The library must have been built (``libmarshal_gb300.build.build()``); there
+is no fallback of any kind: if the CUDA library is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liblmarshal.so")
+
+_lib = None
+_lock = threading.Lock()
+
+
+class LMError(RuntimeError):
+    """A libmarshal_gb300 call returned its error flag."""
+
+
+# name -> (restype, argtypes)
+_B = ctypes.c_bool
+_I = ctypes.c_int
+_LL = ctypes.c_longlong
+_ULLP = ctypes.POINTER(ctypes.c_ulonglong)
+_VP = ctypes.c_void_p
+_SIGS = {
+    "lm_last_error": (ctypes.c_char_p, []),
+    "lm_version": (ctypes.c_char_p, []),
+    "lm_marshal_finalize": (None, []),
+    "cl_marshal_finalize": (None, []),
+    "lm_aos_asta_bs": (_B, [_VP, _VP, _I, _I, _I, _I]),
+    "lm_aos_asta_pttwac": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I]),
+    "lm_aos_asta": (_B, [_VP, _VP, _I, _I, _I, _I, _I]),
+    "lm_transpose": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I, _I, _ULLP]),
+    "lm_transpose_ex": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I, _I, _I, _ULLP]),
+    "lm_transpose_010_bs": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
+    "lm_transpose_010_pttwac": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP, _I, _I]),
+    "lm_transpose_100": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
+    "lm_transpose_0100": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _ULLP]),
+    "lm_transpose_0100_method": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I, _ULLP]),
+    "lm_padding": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
+    "lm_unpadding": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
+    "lm_bs_feasible": (_I, [_LL, _I, _I, _I, _I]),
+    "lm_debug_pad_stall": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _LL,
+                                ctypes.c_ulonglong]),
+    "lm_launch_count": (ctypes.c_ulonglong, []),
+    "lm_prof_enable": (None, [_I]),
+    "lm_prof_collect": (_I, [_VP, _I]),
+    "gpu_aos_asta_bs_float": (_B, [_VP, _I, _I, _I, _VP]),
+    "gpu_aos_asta_bs_double": (_B, [_VP, _I, _I, _I, _VP]),
+    "gpu_aos_asta_pttwac": (_B, [_VP, _I, _I, _I, _VP]),
+    "gpu_soa_asta_pttwac": (_B, [_VP, _I, _I, _I, _VP]),
+}
+
+
+def lib():
+    """Load liblmarshal.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(LIB_PATH):
+                    raise LMError(
+                        "liblmarshal.so is not built (%s); run "
+                        "libmarshal_gb300.build.build()" % LIB_PATH)
+                L = ctypes.CDLL(LIB_PATH)
+                for name, (res, args) in _SIGS.items():
+                    fn = getattr(L, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def last_error() -> str:
+    v = lib().lm_last_error()
+    return v.decode() if v else ""
+
+
+def _check(failed: bool, what: str) -> None:
+    if failed:
+        raise LMError("%s failed: %s" % (what, last_error()))
+
+
+def buf_ptr(buf, elem_bytes=None):
+    """(device pointer, element bytes) of a CUDA tensor or a raw pointer."""
+    if isinstance(buf, int):
+        if elem_bytes is None:
+            raise ValueError("elem_bytes is required with a raw pointer")
+        return buf, int(elem_bytes)
+    if not buf.is_cuda:
+        raise ValueError("buffer must be a CUDA tensor")
+    if not buf.is_contiguous():
+        raise ValueError("buffer must be contiguous")
+    return buf.data_ptr(), int(elem_bytes or buf.element_size())
+
+
+def stream_ptr(stream=None) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class _Timer:
+    def __init__(self, timed):
+        self.v = ctypes.c_ulonglong(0) if timed else None
+
+    def arg(self):
+        return ctypes.byref(self.v) if self.v is not None else None
+
+    def ns(self):
+        return self.v.value if self.v is not None else None
+
+
+def aos_asta_bs(buf, height, width, tile_size, stream=None, elem_bytes=None):
+    p, e = buf_ptr(buf, elem_bytes)
+    _check(lib().lm_aos_asta_bs(stream_ptr(stream), p, e, height, width,
+                                tile_size), "lm_aos_asta_bs")
+
+
+def aos_asta_pttwac(buf, height, width, tile_size, R=1, P=1, stream=None,
+                    elem_bytes=None):
+    p, e = buf_ptr(buf, elem_bytes)
+    _check(lib().lm_aos_asta_pttwac(stream_ptr(stream), p, e, height, width,
+                                    tile_size, R, P), "lm_aos_asta_pttwac")
+
+
+def aos_asta(buf, height, width, tile_size, R=1, stream=None, elem_bytes=None):
+    p, e = buf_ptr(buf, elem_bytes)
+    _check(lib().lm_aos_asta(stream_ptr(stream), p, e, height, width,
+                             tile_size, R), "lm_aos_asta")
+
+
+def transpose(buf, A, a, B, b, R=1, stages=3, variant010=0, stream=None,
+              elem_bytes=None, timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    if variant010:
+        _check(lib().lm_transpose_ex(stream_ptr(stream), p, e, A, a, B, b, R,
+                                     stages, variant010, t.arg()),
+               "lm_transpose_ex")
+    else:
+        _check(lib().lm_transpose(stream_ptr(stream), p, e, A, a, B, b, R,
+                                  stages, t.arg()), "lm_transpose")
+    return t.ns()
+
+
+def transpose_010_bs(buf, A, a, B, stream=None, elem_bytes=None, timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    _check(lib().lm_transpose_010_bs(stream_ptr(stream), p, e, A, a, B,
+                                     t.arg()), "lm_transpose_010_bs")
+    return t.ns()
+
+
+def transpose_010_pttwac(buf, A, a, B, R=1, P=1, stream=None,
+                         elem_bytes=None, timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    _check(lib().lm_transpose_010_pttwac(stream_ptr(stream), p, e, A, a, B,
+                                         t.arg(), R, P),
+           "lm_transpose_010_pttwac")
+    return t.ns()
+
+
+def transpose_100(buf, A, B, b, stream=None, elem_bytes=None, timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    _check(lib().lm_transpose_100(stream_ptr(stream), p, e, A, B, b, t.arg()),
+           "lm_transpose_100")
+    return t.ns()
+
+
+def transpose_0100(buf, A, a, B, b, method=0, stream=None, elem_bytes=None,
+                   timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    if method:
+        _check(lib().lm_transpose_0100_method(stream_ptr(stream), p, e, A, a,
+                                              B, b, method, t.arg()),
+               "lm_transpose_0100_method")
+    else:
+        _check(lib().lm_transpose_0100(stream_ptr(stream), p, e, A, a, B, b,
+                                       t.arg()), "lm_transpose_0100")
+    return t.ns()
+
+
+def padding(buf, x_size, y_size, pad_size, stream=None, elem_bytes=None,
+            timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    _check(lib().lm_padding(stream_ptr(stream), p, e, x_size, y_size, pad_size,
+                            t.arg()), "lm_padding")
+    return t.ns()
+
+
+def unpadding(buf, x_size, y_size, pad_size, stream=None, elem_bytes=None,
+              timed=False):
+    p, e = buf_ptr(buf, elem_bytes)
+    t = _Timer(timed)
+    _check(lib().lm_unpadding(stream_ptr(stream), p, e, x_size, y_size,
+                              pad_size, t.arg()), "lm_unpadding")
+    return t.ns()
+
+
+def bs_feasible(T, a, B, b, elem_bytes) -> bool:
+    return bool(lib().lm_bs_feasible(T, a, B, b, elem_bytes))
+
+
+class ProfEntry(ctypes.Structure):
+    """lm_prof_entry of include/lm_marshal.h."""
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_longlong),
+                ("total_ms", ctypes.c_double)]
+
+
+def launch_count() -> int:
+    """Kernels launched by the library since it was loaded."""
+    return int(lib().lm_launch_count())
+
+
+def prof_enable(on: bool = True) -> None:
+    lib().lm_prof_enable(1 if on else 0)
+
+
+def prof_collect():
+    """{kernel name: (launches, summed device ms)} since the last collect."""
+    cap = 64
+    arr = (ProfEntry * cap)()
+    n = lib().lm_prof_collect(ctypes.cast(arr, ctypes.c_void_p), cap)
+    return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms))
+            for i in range(min(n, cap))}
+
+
+def finalize() -> None:
+    lib().lm_marshal_finalize()

@@ -1,0 +1,355 @@
+"""GPU parity: every elementary op, conversion and staged transposition,
+through the C ABI, bit-exact against the oracle and against golden digests of
+the reference's own CPU code (tests/golden/golden.json)."""
+import ctypes
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import lm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                     "golden.json")))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).tobytes()
+                          ).hexdigest()
+
+
+def make(c, n):
+    if c["fill"] == "index":
+        return O.index_fill(n, c["e"])
+    return O.random_bits(n, c["e"], c["seed"])
+
+
+def to_dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()
+                            ).cuda()
+
+
+def from_dev(t, e):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy().view(O.DTYPES[e])
+
+
+@pytest.fixture(scope="module")
+def L(cuda):
+    from libmarshal_gb300 import lm
+    return lm
+
+
+# ---- AoS <-> ASTA (010) ------------------------------------------------------
+
+@pytest.mark.parametrize("c", GOLDEN["aos_asta"],
+                         ids=lambda c: "%s-%dx%d-t%d-e%d" % (
+                             c["tag"], c["h"], c["w"], c["t"], c["e"]))
+def test_aos_asta_bs_golden(L, c):
+    src = make(c, c["h"] * c["w"])
+    d = to_dev(src)
+    L.aos_asta_bs(d, c["h"], c["w"], c["t"], elem_bytes=c["e"])
+    assert sha(from_dev(d, c["e"])) == c["sha256"]
+
+
+@pytest.mark.parametrize("c", [c for c in GOLDEN["aos_asta"]
+                               if c["tag"] in ("cfg1", "bug525", "bug536",
+                                               "widths")],
+                         ids=lambda c: "%s-%dx%d-t%d-e%d" % (
+                             c["tag"], c["h"], c["w"], c["t"], c["e"]))
+def test_aos_asta_pttwac_golden(L, c):
+    src = make(c, c["h"] * c["w"])
+    d = to_dev(src)
+    L.aos_asta_pttwac(d, c["h"], c["w"], c["t"], R=1, P=1, elem_bytes=c["e"])
+    assert sha(from_dev(d, c["e"])) == c["sha256"]
+
+
+@pytest.mark.parametrize("R", [1, 2, 4, 8, 16])
+def test_010_pttwac_spreading_factors(L, R):
+    # bug536 (test/cl_unittest.cc:225-292): w=197, t=32, S_f = R, P = 1
+    c = [c for c in GOLDEN["aos_asta"] if c["tag"] == "bug536"
+         and c["w"] == 197 and c["t"] == 32][0]
+    src = make(c, c["h"] * c["w"])
+    d = to_dev(src)
+    L.transpose_010_pttwac(d, c["h"] // c["t"], c["t"], c["w"], R=R, P=1,
+                           elem_bytes=4)
+    assert sha(from_dev(d, 4)) == c["sha256"]
+
+
+def test_cuda_dropins_cfg1(L, cuda):
+    import torch
+    c = GOLDEN["aos_asta"][0]
+    assert c["tag"] == "cfg1"
+    lib = L.lib()
+    for fn in ("gpu_aos_asta_bs_float", "gpu_aos_asta_pttwac"):
+        src = make(c, c["h"] * c["w"])
+        d = to_dev(src)
+        assert getattr(lib, fn)(d.data_ptr(), c["h"], c["w"], c["t"], None) \
+            is False, L.last_error()
+        assert sha(from_dev(d, 4)) == c["sha256"], fn
+    # ASTA -> AoS restores the input
+    src = make(c, c["h"] * c["w"])
+    d = to_dev(src)
+    lib.gpu_aos_asta_bs_float(d.data_ptr(), c["h"], c["w"], c["t"], None)
+    L.transpose_010_bs(d, c["h"] // c["t"], c["w"], c["t"], elem_bytes=4)
+    assert np.array_equal(from_dev(d, 4), src)
+    # double variant
+    src8 = O.random_bits(16 * 1024 * 6, 8, 5)
+    d = to_dev(src8)
+    assert lib.gpu_aos_asta_bs_double(d.data_ptr(), 16 * 1024, 6, 16, None) \
+        is False
+    assert np.array_equal(from_dev(d, 8), O.aos_asta(src8, 16 * 1024, 6, 16))
+    # height not a multiple of the tile: error, buffer untouched
+    d = to_dev(src)
+    assert lib.gpu_aos_asta_bs_float(d.data_ptr(), 1000, 7, 33, None) is True
+    assert np.array_equal(from_dev(d, 4), src)
+    torch.cuda.synchronize()
+
+
+# ---- SoA -> ASTA (100) -------------------------------------------------------
+
+@pytest.mark.parametrize("c", GOLDEN["soa_asta"],
+                         ids=lambda c: "%s-%dx%d-t%d-e%d" % (
+                             c["tag"], c["h"], c["w"], c["t"], c["e"]))
+def test_soa_asta_golden(L, c):
+    src = make(c, c["h"] * c["w"])
+    d = to_dev(src)
+    if c["e"] == 4:
+        assert L.lib().gpu_soa_asta_pttwac(d.data_ptr(), c["h"], c["w"],
+                                           c["t"], None) is False
+    else:
+        L.transpose_100(d, c["w"], c["h"] // c["t"], c["t"],
+                        elem_bytes=c["e"])
+    assert sha(from_dev(d, c["e"])) == c["sha256"]
+
+
+# ---- full transposition (staged planner) -------------------------------------
+
+@pytest.mark.parametrize("c", GOLDEN["full"],
+                         ids=lambda c: "%s-%dx%d-e%d" % (c["tag"], c["M"],
+                                                         c["N"], c["e"]))
+def test_full_transpose_planner_golden(L, c):
+    M, N, e = c["M"], c["N"], c["e"]
+    A, a, B, b, ph, pw = O.alg5(M, N)
+    src = make(c, M * N)
+    d = to_dev(src)
+    if ph == 0 and pw == 0:
+        stages = O.alg3(A, a, B, b)
+        L.transpose(d, A, a, B, b, R=1, stages=stages, elem_bytes=e)
+    else:
+        L.transpose(d, M, 1, N, 1, R=1, stages=0, elem_bytes=e)
+    assert sha(from_dev(d, e)) == c["sha256"]
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+@pytest.mark.parametrize("stages", [2, 22, 3, 32, 4, 0])
+@pytest.mark.parametrize("variant", [1, 2])
+def test_cfg2_every_stage_and_variant(L, e, stages, variant):
+    # BASELINE 7200x1800 with index fill; a=100, A=72, b=100, B=18
+    c = [c for c in GOLDEN["full"] if c["tag"] == "cfg2" and c["e"] == e][0]
+    src = make(c, 7200 * 1800)
+    d = to_dev(src)
+    # the 010 steps each stage runs: (tiles, a, B)
+    steps010 = {2: [(72, 100, 1800)], 22: [(18, 7200, 100)],
+                3: [(1296, 100, 100)], 32: [(1296, 100, 100)],
+                4: [(1296, 100, 100)], 0: []}[stages]
+    if variant == 1 and not all(L.bs_feasible(T, a, B, 1, e)
+                                for (T, a, B) in steps010):
+        # forcing BS on a tile that cannot be staged on chip is an error,
+        # as in the reference past MAX_MEM
+        from libmarshal_gb300.lm import LMError
+        with pytest.raises(LMError):
+            L.transpose(d, 72, 100, 18, 100, R=1, stages=stages,
+                        variant010=variant, elem_bytes=e)
+        return
+    L.transpose(d, 72, 100, 18, 100, R=1, stages=stages, variant010=variant,
+                elem_bytes=e)
+    assert sha(from_dev(d, e)) == c["sha256"]
+
+
+# ---- exhaustive small shapes, every width and method ------------------------
+
+def small_shapes(seed, count):
+    rng = np.random.default_rng(seed)
+    out = [(1, 1, 1, 1), (0, 3, 4, 5), (2, 1, 7, 3), (2, 7, 1, 3),
+           (1, 2, 3, 1), (3, 16, 16, 1), (1, 33, 65, 2), (5, 4, 3, 1000),
+           (1, 3, 5, 2049)]
+    for _ in range(count):
+        A = int(rng.integers(1, 6))
+        a = int(rng.integers(1, 40))
+        B = int(rng.integers(1, 40))
+        b = int(rng.choice([1, 1, 2, 3, 4, 7, 16, 33, 64, 100]))
+        out.append((A, a, B, b))
+    return out
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_0100_small_shapes(L, e, method):
+    for (A, a, B, b) in small_shapes(100 * e + method, 60):
+        n = A * a * B * b
+        src = O.random_bits(max(n, 1), e, A + a + B + b)[:n]
+        d = to_dev(src) if n else None
+        if n == 0:
+            import torch
+            d = torch.zeros(8, dtype=torch.uint8, device="cuda")
+            L.transpose_0100(d, A, a, B, b, method=method, elem_bytes=e)
+            continue
+        L.transpose_0100(d, A, a, B, b, method=method, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), O.t0100(src, A, a, B, b)), \
+            (A, a, B, b, e, method)
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_unaligned_buffers(L, e):
+    import torch
+    for (A, B, b) in ((37, 29, 32), (64, 48, 16), (100, 77, 3)):
+        n = A * B * b
+        src = O.random_bits(n, e, 9)
+        big = torch.zeros((n + 16) * e, dtype=torch.uint8, device="cuda")
+        off = e  # one element past the allocation's alignment
+        big[off:off + n * e] = to_dev(src)
+        ptr = big.data_ptr() + off
+        assert L.lib().lm_transpose_100(None, ptr, e, A, B, b, None) is False, \
+            L.last_error()
+        got = big[off:off + n * e].cpu().numpy().view(O.DTYPES[e])
+        assert np.array_equal(got, O.t100(src, A, B, b))
+
+
+def test_large_tiles_use_clusters(L):
+    # 010 tiles of 32 x 12289 fp32 (1.57 MB) and 16 x 16000 fp64 (2 MB)
+    for (A, a, B, e) in ((3, 32, 12289, 4), (2, 16, 16000, 8),
+                         (4, 8, 30000, 4)):
+        assert L.bs_feasible(A, a, B, 1, e)
+        src = O.random_bits(A * a * B, e, 1)
+        d = to_dev(src)
+        L.transpose_010_bs(d, A, a, B, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), O.t010(src, A, a, B))
+
+
+def test_bs_reports_capacity_error(L):
+    # a 2 x 2^21 fp64 tile (32 MB) cannot be staged on chip
+    from libmarshal_gb300.lm import LMError
+    import torch
+    d = torch.zeros(2 * (1 << 21) * 8, dtype=torch.uint8, device="cuda")
+    with pytest.raises(LMError):
+        L.transpose_010_bs(d, 1, 2, 1 << 21, elem_bytes=8)
+    # the planner / PTTWAC path handles it
+    src = O.random_bits(2 * (1 << 21), 8, 4)
+    d = to_dev(src)
+    L.transpose_0100(d, 1, 2, 1 << 21, 1, elem_bytes=8)
+    assert np.array_equal(from_dev(d, 8), O.t010(src, 1, 2, 1 << 21))
+
+
+# ---- padding -----------------------------------------------------------------
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_padding_unpadding(L, e):
+    import torch
+    rng = np.random.default_rng(e)
+    shapes = [(1000, 1001, 1003), (12289, 300, 12291), (5, 70000, 9),
+              (3, 2, 3), (64, 64, 64), (1, 100000, 2)]
+    for _ in range(6):
+        x = int(rng.integers(1, 3000))
+        y = int(rng.integers(1, 3000))
+        shapes.append((x, y, x + int(rng.integers(0, 40))))
+    for (x, y, pad) in shapes:
+        buf = O.random_bits(y * pad, e, x + y)
+        d = to_dev(buf)
+        L.padding(d, x, y, pad, elem_bytes=e)
+        got = from_dev(d, e)
+        want = O.padding(buf, x, y, pad)
+        assert np.array_equal(got, want), ("pad", x, y, pad, e)
+        L.unpadding(d, x, y, pad, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), O.unpadding(want, x, y, pad)), \
+            ("unpad", x, y, pad, e)
+    torch.cuda.synchronize()
+
+
+def test_pad_transpose_unpad_flow(L):
+    # The reference's `full` test flow (test/cl_unittest.cc:396-640): pad the
+    # columns to a factorable width, transpose, unpad; 1000 x 1009 (prime).
+    h, w = 1000, 1009
+    A, a, B, b, ph, pw = O.alg5(h, w)
+    H, W = h + ph, w + pw
+    src = O.random_bits(h * w, 4, 77)
+    buf = np.zeros(H * W, dtype=np.uint32)
+    buf[:h * w] = src
+    d = to_dev(buf)
+    if pw:
+        L.padding(d, w, h, W, elem_bytes=4)
+    L.transpose(d, A, a, B, b, R=1, stages=O.alg3(A, a, B, b), elem_bytes=4)
+    if ph:
+        L.unpadding(d, h, w, H, elem_bytes=4)
+    else:
+        L.unpadding(d, h, w, H, elem_bytes=4)  # H == h: keeps first w rows
+    got = from_dev(d, 4)[:h * w]
+    assert np.array_equal(got, O.transpose(src, h, w))
+
+
+# ---- failure detection without a GPU fault -----------------------------------
+
+@pytest.mark.parametrize("unpad", [0, 1])
+def test_bounded_wait_reports_timeout(L, unpad):
+    import torch
+    x, y, pad = 1000, 2000, 1010
+    buf = O.random_bits(y * pad, 4, 1)
+    d = to_dev(buf)
+    failed = L.lib().lm_debug_pad_stall(None, d.data_ptr(), 4, x, y, pad,
+                                        unpad, 3, 50_000_000)
+    assert failed is True
+    assert "timed out" in L.last_error()
+    # the context is still usable
+    d2 = to_dev(buf)
+    L.padding(d2, x, y, pad, elem_bytes=4)
+    assert np.array_equal(from_dev(d2, 4), O.padding(buf, x, y, pad))
+    torch.cuda.synchronize()
+
+
+# ---- Python API (src/py/transpose.py) ----------------------------------------
+
+def test_python_array_api(L):
+    import torch
+    from libmarshal_gb300 import TransposeArrayInPlace, FullTranspose, T010_BS
+    # transpose_unittest.py:82-94 shape
+    A, a, B, b = 40, 16, 37, 10
+    src = O.random_bits(A * a * B * b, 4, 3).reshape(A * a, B * b)
+    t = torch.from_numpy(src.view(np.float32).copy()).cuda()
+    out = TransposeArrayInPlace(t, a, b)
+    assert tuple(out.shape) == (B * b, A * a)
+    assert out.data_ptr() == t.data_ptr()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), src.T)
+    # transpose_unittest.py:39-57
+    for a in (4, 8, 16, 32, 64):
+        src = O.random_bits(40 * a * 37 * 30, 4, a)
+        t = torch.from_numpy(src.view(np.float32).copy()).cuda()
+        steps = FullTranspose(None, t, 40, a, 37, 30)
+        torch.cuda.synchronize()
+        assert np.array_equal(t.cpu().numpy().view(np.uint32),
+                              O.transpose(src, 40 * a, 37 * 30))
+        assert all(s.Throughput() > 0 for s in steps)
+    # transpose_unittest.py:59-80
+    for a in (4, 8, 16, 32, 64):
+        src = O.random_bits(40 * a * 37, 4, a + 1)
+        t = torch.from_numpy(src.view(np.float32).copy()).cuda()
+        op = T010_BS(40, a, 37)
+        assert op.IsFeasible(t)
+        op.Transpose(None, t)
+        assert op.Throughput() > 0
+        assert np.array_equal(t.cpu().numpy().view(np.uint32),
+                              O.t010(src, 40, a, 37))
+
+
+def test_elapsed_time_accumulates(L):
+    src = O.random_bits(1024 * 999, 4, 2)
+    d = to_dev(src)
+    et = ctypes.c_ulonglong(5)
+    assert L.lib().lm_transpose_100(None, d.data_ptr(), 4, 1024, 999, 1,
+                                    ctypes.byref(et)) is False
+    assert et.value > 5

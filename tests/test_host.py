@@ -1,0 +1,96 @@
+"""Host-side checks that need no GPU: the C ABI library builds, loads and
+exports every symbol include/*.h declares; the division helper used by every
+kernel; the Python API's host logic."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = set()
+    for h in ("marshal.h", "lm_marshal.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?\w+\s*\**\s*(\w+)\s*\(",
+                             text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_the_reference_surface():
+    names = header_functions()
+    # include/marshal.h:26-31 of the reference
+    for n in ("gpu_aos_asta_bs_float", "gpu_aos_asta_bs_double",
+              "gpu_aos_asta_pttwac", "gpu_soa_asta_pttwac"):
+        assert n in names
+    # include/cl_marshal.h:26-49 of the reference, lm_ prefix
+    for n in ("aos_asta_bs", "aos_asta_pttwac", "aos_asta", "transpose",
+              "transpose_010_bs", "transpose_010_pttwac", "transpose_100",
+              "transpose_0100", "padding", "unpadding"):
+        assert "lm_" + n in names
+    assert "cl_marshal_finalize" in names
+
+
+def test_library_exports_every_declared_symbol(built):
+    from libmarshal_gb300 import lm
+    L = lm.lib()
+    for name in header_functions():
+        assert hasattr(L, name), name
+    assert set(header_functions()) <= set(lm.exported_symbols())
+    assert b"sm_103a" in L.lm_version()
+
+
+def test_library_reports_errors_without_a_gpu_call(built):
+    # argument validation happens before any CUDA call
+    from libmarshal_gb300 import lm
+    L = lm.lib()
+    assert L.lm_aos_asta_bs(None, None, 4, 10, 3, 4) is True
+    assert "multiple" in lm.last_error()
+    assert L.lm_transpose_100(None, None, 3, 4, 5, 1, None) is True
+    assert "element size" in lm.last_error()
+
+
+def _fastdiv(d):
+    l = 0
+    while l < 32 and (1 << l) < d:
+        l += 1
+    m = ((1 << 32) * ((1 << l) - d)) // d + 1
+    return m & 0xffffffff, l
+
+
+def test_fastdiv_formula():
+    # Python restatement of lm::make_fastdiv / lm::fdiv (lm_core.cuh)
+    rng = np.random.default_rng(0)
+    ds = [1, 2, 3, 5, 7, 31, 32, 33, 100, 12289, 16384, 65537, 2**31 - 1,
+          2**31, 2**31 + 1, 2**32 - 1] + [int(v) for v in
+                                          rng.integers(1, 2**32, size=200)]
+    ns = [0, 1, 2**31 - 1, 2**31, 2**32 - 1] + [int(v) for v in
+                                                rng.integers(0, 2**32,
+                                                             size=300)]
+    for d in ds:
+        m, s = _fastdiv(d)
+        assert m < 2**32
+        for n in ns + [d - 1, d, d + 1, (2**32 - 1) // d * d]:
+            if not 0 <= n < 2**32:
+                continue
+            hi = (n * m) >> 32
+            assert (hi + n) >> s == n // d, (n, d)
+
+
+def test_python_api_host_logic():
+    from libmarshal_gb300 import Transposition, TransposeArrayInPlace
+    from oracle import lm_oracle as O
+    for m, n in ((2, 3), (3, 5), (7, 4), (12, 9)):
+        t = Transposition(m, n)
+        assert t.GetNumCycles() == O.num_cycles(m, n)
+        for i in range(m * n):
+            assert t.Next(i) == O.next_index(i, m, n)
+    torch = pytest.importorskip("torch")
+    with pytest.raises(TypeError):
+        TransposeArrayInPlace(torch.zeros(2, 3, 4))
+    with pytest.raises(TypeError):
+        TransposeArrayInPlace(torch.zeros(10, 9), a=3, b=1)
