@@ -112,6 +112,23 @@ bool lm_padding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
 bool lm_unpadding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
                   int y_size, int pad_size, unsigned long long *et);
 
+/* 100 [A][B][b] -> [B][A][b] like lm_transpose_100, for callers that cannot
+ * allocate device memory while they run -- for example an allocator or
+ * memory manager converting layouts from inside its own allocation path
+ * (calling cudaMalloc there would re-enter it), or a real-time pipeline that
+ * reserves all device memory at start-up.  No counterpart in the reference.
+ * It allocates nothing: its scratch (one done bit per unit) is a fixed 4 MiB
+ * device array that every GPU loading this library keeps until exit, so a
+ * call handles at most 33,554,432 units (a unit larger than one slice, at
+ * most 4 KiB, counts once per slice); larger shapes return true with an
+ * error.  All calls on a
+ * device share that array (each clears what it uses first): calls that
+ * overlap on the GPU race -- order them on one stream.  The first call on a
+ * device looks the array up (with that device current); make it before any
+ * stream capture.  Asynchronous, stream ordered; false on success. */
+bool lm_transpose_100_noalloc(lm_stream_t stream, void *buf, int elem_bytes,
+                              int A, int B, int b);
+
 /* 1 when a 0100 tile [a][B][b] (T tiles) of elem_bytes elements can be staged
  * on chip (shared memory of one CTA or of a thread-block cluster), else 0.
  * Counterpart of T010_BS::IsFeasible (include/plan.hpp:108-111). */

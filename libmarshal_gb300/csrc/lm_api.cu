@@ -69,6 +69,8 @@ static bool fail(const char *fmt, ...) {
   return true;
 }
 
+bool set_error(const char *msg) { return fail("%s", msg); }
+
 static bool cuda_fail(cudaError_t e, const char *what) {
   return fail("%s: %s", what, cudaGetErrorString(e));
 }

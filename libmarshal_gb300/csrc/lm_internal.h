@@ -18,6 +18,9 @@ struct DeviceInfo {
 };
 const DeviceInfo &device_info();  // current device, cached
 
+// Records `msg` as the calling thread's lm_last_error(); returns true.
+bool set_error(const char *msg);
+
 // Every kernel launch of the library is wrapped in a ProfScope: it counts the
 // launch and, while profiling is on (lm_prof_enable), records a CUDA event
 // pair around it on the launching stream (lm_prof.cu).

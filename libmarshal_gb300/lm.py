@@ -44,6 +44,7 @@ _SIGS = {
     "lm_transpose_010_bs": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
     "lm_transpose_010_pttwac": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP, _I, _I]),
     "lm_transpose_100": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
+    "lm_transpose_100_noalloc": (_B, [_VP, _VP, _I, _I, _I, _I]),
     "lm_transpose_0100": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _ULLP]),
     "lm_transpose_0100_method": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I, _ULLP]),
     "lm_padding": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
