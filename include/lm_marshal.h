@@ -97,8 +97,12 @@ bool lm_transpose_100(lm_stream_t stream, void *buf, int elem_bytes, int A,
 bool lm_transpose_0100(lm_stream_t stream, void *buf, int elem_bytes, int A,
                        int a, int B, int b, unsigned long long *et);
 /* 0100 with the algorithm forced: 0 = planner, 1 = BS (on-chip tiles),
- * 2 = PTTWAC on b-element units.  No reference counterpart (the reference
- * picks by super-element size, cl_marshal.cc:365-370). */
+ * 2 = PTTWAC on b-element units, 3 = stash (A == 1 only: save the half that
+ * is overwritten first, then a streaming wavefront), 4 = two passes (BS on
+ * tiles that make >= 128-byte units, then PTTWAC on those units).  Returns
+ * true when the forced algorithm does not apply to the shape.  No reference
+ * counterpart (the reference picks by super-element size,
+ * cl_marshal.cc:365-370). */
 bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
                               int A, int a, int B, int b, int method,
                               unsigned long long *et);
@@ -128,6 +132,12 @@ bool lm_unpadding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
  * stream capture.  Asynchronous, stream ordered; false on success. */
 bool lm_transpose_100_noalloc(lm_stream_t stream, void *buf, int elem_bytes,
                               int A, int B, int b);
+
+/* Waits for `stream`, then returns and clears the accumulated failure status
+ * of this device's waiting kernels (0 = ok, 1 = an inter-CTA wait timed out).
+ * Asynchronous calls (et == NULL) report such failures only here; timed calls
+ * (et != NULL) check it themselves.  No reference counterpart. */
+unsigned lm_device_status(lm_stream_t stream);
 
 /* 1 when a 0100 tile [a][B][b] (T tiles) of elem_bytes elements can be staged
  * on chip (shared memory of one CTA or of a thread-block cluster), else 0.

@@ -111,6 +111,38 @@ static bool get_zeroed(Scratch &sc, size_t bytes, cudaStream_t s) {
   return false;
 }
 
+// ---- persistent status word (failures of waiting kernels) ---------------
+
+uint32_t *device_status_word() {
+  static std::mutex mu;
+  static uint32_t *words[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!words[dev]) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, 4) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, 4) != cudaSuccess) return nullptr;
+    words[dev] = (uint32_t *)p;
+  }
+  return words[dev];
+}
+
+// Reads and clears the status word after the stream's work has finished.
+static bool check_status(cudaStream_t s, const char *what) {
+  uint32_t *w = device_status_word();
+  if (!w) return fail("%s: no status word", what);
+  uint32_t v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, w, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  if (v != kStatusOk) {
+    cudaMemsetAsync(w, 0, 4, s);
+    return fail("%s: an inter-CTA wait timed out (status %u)", what, v);
+  }
+  return false;
+}
+
 // ---- timing (the reference's elapsed_time accumulator) ----------------------
 
 struct OpTimer {
@@ -130,6 +162,7 @@ struct OpTimer {
     cudaEventRecord(b, s);
     cudaError_t e = cudaEventSynchronize(b);
     if (e != cudaSuccess) return cuda_fail(e, "timing");
+    if (check_status(s, "status")) return true;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     *et += (unsigned long long)((double)ms * 1.0e6);
@@ -143,9 +176,16 @@ struct OpTimer {
 
 static bool valid_e(int e) { return e == 1 || e == 2 || e == 4 || e == 8; }
 
+// Limit for every inter-CTA wait (LM_WAIT_TIMEOUT_MS overrides, default 2 s).
+static uint64_t wait_timeout_ns() {
+  const char *v = getenv("LM_WAIT_TIMEOUT_MS");
+  const long long ms = v ? atoll(v) : 2000;
+  return (uint64_t)(ms > 0 ? ms : 2000) * 1000000ull;
+}
+
 // ---- planner ----------------------------------------------------------------
 
-enum class Method { Auto, BS, Pttwac };
+enum class Method { Auto, BS, Pttwac, Stash, TwoPass };
 
 static bool check_launch(cudaError_t e, const char *what) {
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -201,7 +241,7 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   if (a == 1 || B == 1) return false;                      // identity
   if (buf == nullptr) return fail("null buffer");
   if (a * B >= 0xffffffffull) return fail("a*B must be < 2^32");
-  if (m != Method::Pttwac) {
+  if (m == Method::Auto || m == Method::BS) {
     BsPlan p = plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e);
     if (p.feasible)
       return check_launch(launch_bs0100(s, buf, e, T, (uint32_t)a,
@@ -212,21 +252,42 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
                   (unsigned long long)(a * B * b * e));
   }
   const uint64_t U = b * e;
-  if (m == Method::Auto && U < 128) {
+  const bool want_stash =
+      m == Method::Stash ||
+      (m == Method::Auto && T == 1 && U < 128 && a * B >= (1ull << 20) &&
+       !getenv("LM_NO_STASH"));
+  if (want_stash) {
+    // 100 on small units: the 3 x payload streaming plan (lm_stash.cu).
+    StashPlan sp = T == 1 ? plan_stash(a, B, (uint32_t)b, e) : StashPlan();
+    uint32_t *status = sp.feasible ? device_status_word() : nullptr;
+    if (sp.feasible && status) {
+      Scratch sc;
+      if (get_zeroed(sc, stash_scratch_bytes(sp), s)) return true;
+      return check_launch(launch_stash100(s, buf, e, a, B, (uint32_t)b, sp,
+                                          sc.p, status, wait_timeout_ns()),
+                          "stash launch");
+    }
+    if (m == Method::Stash)
+      return fail("stash plan not applicable to 0100(%llu, %llu, %llu, %llu)",
+                  (unsigned long long)T, (unsigned long long)a,
+                  (unsigned long long)B, (unsigned long long)b);
+  }
+  if ((m == Method::Auto && U < 128) || m == Method::TwoPass) {
     // Aggregate small super-elements into >=128-byte units first so the
     // cycle-following pass moves whole cache lines.
     uint64_t a2 = split_a(a, B, b, e);
     if (a2) {
       const uint64_t a1 = a / a2;
       if (do_0100(s, buf, e, T * a1, a2, B, b, Method::BS)) return true;
-      return do_0100(s, buf, e, T, a1, B, a2 * b, Method::Auto);
+      return do_0100(s, buf, e, T, a1, B, a2 * b, Method::Pttwac);
     }
     uint64_t c = split_B(a, B, b, e);
     if (c) {
       const uint64_t B1 = B / c;
-      if (do_0100(s, buf, e, T, a, B1, c * b, Method::Auto)) return true;
+      if (do_0100(s, buf, e, T, a, B1, c * b, Method::Pttwac)) return true;
       return do_0100(s, buf, e, T * B1, a, c, b, Method::BS);
     }
+    if (m == Method::TwoPass) return fail("no two-pass split for this shape");
   }
   return run_pttwac_direct(s, buf, e, T, a, B, b);
 }
@@ -388,7 +449,12 @@ bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
                               unsigned long long *et) {
   OpTimer t(et, (cudaStream_t)stream);
   if (A < 0 || a < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
-  Method m = method == 1 ? Method::BS : method == 2 ? Method::Pttwac : Method::Auto;
+  if (method < 0 || method > 4) return fail("method must be 0..4");
+  const Method m = method == 1   ? Method::BS
+                   : method == 2 ? Method::Pttwac
+                   : method == 3 ? Method::Stash
+                   : method == 4 ? Method::TwoPass
+                                 : Method::Auto;
   if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
               (uint64_t)B, (uint64_t)b, m))
     return true;
@@ -465,6 +531,20 @@ bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
                         long long stall_block, unsigned long long timeout_ns) {
   return do_pad((cudaStream_t)stream, buf, elem_bytes, x_size, y_size,
                 pad_size, unpad == 0, timeout_ns, stall_block);
+}
+
+// Waits for `stream` and returns (then clears) the accumulated status of
+// waiting kernels on the current device: 0 = ok.
+unsigned lm_device_status(lm_stream_t stream) {
+  uint32_t *w = device_status_word();
+  if (!w) return 0xffffffffu;
+  uint32_t v = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(&v, w, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return 0xffffffffu;
+  if (v) cudaMemsetAsync(w, 0, 4, s);
+  return v;
 }
 
 // Planner query used by the Python API's IsFeasible(): 1 when the 0100 tile

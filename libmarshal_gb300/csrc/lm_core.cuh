@@ -21,7 +21,7 @@ struct FastDiv {
   uint32_t shift;
 };
 
-inline FastDiv make_fastdiv(uint32_t d) {
+__host__ __device__ inline FastDiv make_fastdiv(uint32_t d) {
   FastDiv f;
   f.d = d ? d : 1;
   uint32_t l = 0;
@@ -34,6 +34,10 @@ inline FastDiv make_fastdiv(uint32_t d) {
 __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
   const uint32_t hi = __umulhi(n, f.mul);
   return (uint32_t)(((uint64_t)hi + n) >> f.shift);
+}
+
+__host__ __device__ __forceinline__ uint64_t min64(uint64_t a, uint64_t b) {
+  return a < b ? a : b;
 }
 
 // Vector type of V bytes.
@@ -83,11 +87,73 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
   return t;
 }
 
+// ---- shared-memory barriers and bulk (TMA) copies ---------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Orders this thread's earlier generic-proxy shared accesses before later
+// async-proxy (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
+                                                      uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::
+          "r"(smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared (the TMA engine); addresses and size must be
+// multiples of 16 bytes; completion is signalled on `bar` as transaction bytes.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // Status word written by kernels that wait on other CTAs; the host turns a
 // non-zero value into an error return.
 enum : uint32_t {
   kStatusOk = 0,
   kStatusWaitTimeout = 1,
+  kStatusBadLayout = 2,  // a kernel refused an unaligned bulk copy
 };
 
 }  // namespace lm

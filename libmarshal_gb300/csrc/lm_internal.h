@@ -74,6 +74,30 @@ cudaError_t launch_pttwac010_smem(cudaStream_t s, void *buf, int e,
                                   uint64_t A, uint32_t a, uint32_t B, int R,
                                   int P);
 
+// ---- 100 for small units with 3 x payload traffic (lm_stash.cu) ---------
+// K1 saves the half of the matrix that is overwritten before it is read; K2
+// is a persistent wavefront over column groups with per-chunk progress
+// counters and bounded waits (status word on timeout).
+struct StashPlan {
+  bool feasible = false;
+  uint32_t g = 0, G = 0;       // units per column group, groups
+  uint32_t W = 0, nchunks = 0; // rows per chunk, chunks (= CTAs)
+  uint32_t pitch = 0;          // shared bytes per gathered row
+  size_t smem_bytes = 0;
+  int ctas_per_sm = 1;
+  size_t stash_bytes = 0;
+};
+StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e);
+size_t stash_scratch_bytes(const StashPlan &p);  // zeroed scratch to pass
+cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
+                            uint64_t B, uint32_t b, const StashPlan &p,
+                            void *scratch, uint32_t *status,
+                            uint64_t timeout_ns);
+
+// Per-device persistent status word that waiting kernels OR their failures
+// into (allocated on first use); lm_api.cu reads and clears it.
+uint32_t *device_status_word();
+
 // ---- row padding / unpadding with bounded inter-CTA waits ----------------
 // padding:   [y][x] -> [y][pad] (new columns zero)
 // unpadding: [y][pad] -> [y][x], tail y*x..y*pad-1 zero.

@@ -1,0 +1,500 @@
+// lm_stash.cu -- in-place 100 for small super-elements with 3 x payload traffic.
+//
+// The reference moves small super-elements by cycle following
+// (_transpose_100, src/cl/cl_aos_asta.cl:352-569): for the plain transpose
+// (b = 1) every step is a dependent 4-byte access.  Cycle following on
+// cache-line units needs a preceding 010 pass, i.e. two full passes (4 x
+// payload bytes).  This file implements a streaming alternative that moves
+// 3 x payload bytes and only touches memory in >= 128-byte runs:
+//
+//   [A][B] units -> [B][A].  Destination rows are produced in groups of g
+//   (one group = g source columns, a column strip of the source) in order
+//   J = 0, 1, ...; group J's destination region D_J is the address range
+//   [g*J*A, g*(J+1)*A) of the buffer.  A source unit at address x = i*B + j
+//   is overwritten when its region J(x) = x / (g*A) is written and consumed
+//   when its column group j / g is gathered.  Units whose region comes first
+//   must be saved: for group J these are exactly the rows i < r(J) =
+//   ceil(g*J*(A-1)/B) (half of the matrix over all J).
+//
+//   K1 (k_stash_save): copies rows i < r(J) of every column group J into a
+//   compact stash (stream-ordered scratch): reads and writes half the data.
+//   K2 (k_stash_wave): a persistent grid; CTA c owns the source rows
+//   [c*W, (c+1)*W).  For each J it gathers its rows' group-J strip (from the
+//   stash for i < r(J), from the buffer otherwise) into shared memory,
+//   publishes progress[c] = J+1, waits until every CTA whose rows hold
+//   original data inside its destination range has gathered group J, and
+//   writes its W units into each of the g destination rows.  Every wait is
+//   on a CTA that never waits for a later step, so the waits end; each one
+//   is also bounded by %globaltimer and reports through a status word.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
+#include "lm_core.cuh"
+#include "lm_internal.h"
+
+namespace lm {
+
+struct StashArgs {
+  char *base;
+  char *stash;
+  const uint64_t *soff;  // byte offset of each group's stash block, G+1
+  uint32_t *progress;    // one counter per row chunk
+  uint32_t *status;
+  uint64_t A, B;         // rows, columns (units)
+  uint32_t b;            // elements per unit
+  uint32_t g;            // units per column group
+  uint32_t G;            // groups
+  uint32_t W;            // rows per chunk
+  uint32_t nchunks;
+  uint32_t pitch;        // shared bytes per gathered row
+  uint32_t gb;           // g*b elements per full strip row
+  FastDiv div_gb;
+  FastDiv div_b;
+  uint64_t timeout_ns;
+};
+
+// Bytes of one ring stage: W rows of `pitch` bytes, then W uint32 row
+// offsets; rounded to 128 so every stage (a bulk-copy destination) stays
+// 16-byte aligned.
+__host__ __device__ __forceinline__ size_t stash_stage_bytes(uint64_t W,
+                                                             uint32_t pitch) {
+  return (size_t)((W * pitch + W * 4 + 127) / 128 * 128);
+}
+
+__host__ __device__ __forceinline__ uint64_t stash_rows(uint64_t J, uint64_t g,
+                                                        uint64_t A,
+                                                        uint64_t B) {
+  // r(J) = ceil(g*J*(A-1)/B), at most A
+  const uint64_t num = g * J * (A - 1);
+  const uint64_t r = (num + B - 1) / B;
+  return r < A ? r : A;
+}
+
+// K0: stash offsets (one thread per group, then a single-block scan).
+__global__ void k_stash_offsets(uint64_t *soff, uint64_t A, uint64_t B,
+                                uint32_t g, uint32_t G, uint64_t row_bytes) {
+  __shared__ uint64_t part[1024];
+  const uint32_t t = threadIdx.x, nt = blockDim.x;
+  const uint32_t per = (G + nt - 1) / nt;
+  const uint32_t j0 = min(G, t * per), j1 = min(G, j0 + per);
+  uint64_t s = 0;
+  for (uint32_t J = j0; J < j1; ++J) s += stash_rows(J, g, A, B) * row_bytes;
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    uint64_t acc = 0;
+    for (uint32_t i = 0; i < nt; ++i) {
+      const uint64_t v = part[i];
+      part[i] = acc;
+      acc += v;
+    }
+    soff[G] = acc;
+  }
+  __syncthreads();
+  uint64_t acc = part[t];
+  for (uint32_t J = j0; J < j1; ++J) {
+    soff[J] = acc;
+    acc += stash_rows(J, g, A, B) * row_bytes;
+  }
+}
+
+// K1: copy the rows that are overwritten before they are consumed.
+// grid.x: row blocks of kSaveRows rows, grid.y: column groups.
+constexpr uint32_t kSaveRows = 32;
+constexpr int kSaveThreads = 256;
+
+template <int E>
+__global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
+  using T = typename Elem<E>::T;
+  const uint32_t J = blockIdx.y;
+  const uint64_t r = stash_rows(J, g.g, g.A, g.B);
+  const uint64_t i0 = (uint64_t)blockIdx.x * kSaveRows;
+  if (i0 >= r) return;
+  const uint32_t nrows = (uint32_t)min64(kSaveRows, r - i0);
+  const uint64_t col0 = (uint64_t)J * g.g;
+  const uint32_t gj = (uint32_t)min64(g.g, g.B - col0);
+  const uint32_t n_row = gj * g.b;  // elements per row strip
+  const uint32_t n = nrows * g.gb;
+  const T *src = reinterpret_cast<const T *>(g.base);
+  T *dst = reinterpret_cast<T *>(g.stash + g.soff[J]) + i0 * g.gb;
+  for (uint32_t t = threadIdx.x; t < n; t += kSaveThreads * 4) {
+    T v[4];
+    uint32_t k[4];
+    uint64_t row[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t tt = t + u * kSaveThreads;
+      const uint32_t rr = fdiv(tt, g.div_gb);
+      k[u] = tt - rr * g.gb;
+      row[u] = i0 + rr;
+      if (tt < n && k[u] < n_row)
+        v[u] = __ldcg(src + (row[u] * g.B + col0) * g.b + k[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t tt = t + u * kSaveThreads;
+      if (tt < n && k[u] < n_row) __stcg(dst + tt, v[u]);
+    }
+  }
+}
+
+// K2: the wavefront, warp-specialised.  Per CTA:
+//   warp 0 (producer): gathers step J into ring stage J % kStages with 1-D
+//     bulk copies (TMA), one per row, each a 16-byte aligned superset of the
+//     row strip (rowoff[] records where the strip starts);
+//   warp 1 (poller): when stage J has landed, publishes progress = J+1, then
+//     waits for the CTAs whose rows hold original data in its destination
+//     range and releases the stage to the writers;
+//   warps 2.. (writers): write step J from the stage, then free it.
+// Stages are handed over with mbarriers (full / ready / empty); every wait is
+// bounded by %globaltimer; a timeout sets the status word and all roles stop.
+constexpr int kWaveThreads = 512;
+constexpr int kStages = 3;
+constexpr int kWriterWarps = kWaveThreads / 32 - 2;
+
+template <int E>
+__global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
+  using T = typename Elem<E>::T;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[kStages], ready[kStages],
+      empty[kStages];
+  __shared__ volatile int s_ok;
+  const uint32_t ch = blockIdx.x;
+  const uint64_t i0 = (uint64_t)ch * g.W;
+  if (i0 >= g.A) return;
+  const uint32_t Wc = (uint32_t)min64(g.W, g.A - i0);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t U = g.b * E;
+  // stage s: rows at smem + s*stage_sz, row offsets (uint32) after the rows
+  const size_t rows_sz = (size_t)g.W * g.pitch;
+  const size_t stage_sz = stash_stage_bytes(g.W, g.pitch);
+  auto stage = [&](uint32_t s) { return smem + s * stage_sz; };
+  auto rowoff = [&](uint32_t s) {
+    return reinterpret_cast<uint32_t *>(smem + s * stage_sz + rows_sz);
+  };
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&ready[s], 1);
+      mbar_init(&empty[s], kWriterWarps);
+    }
+    fence_mbar_init();
+    s_ok = 1;
+  }
+  __syncthreads();
+
+  // bounded wait; false on timeout or when another role has failed
+  auto wait_bar = [&](uint64_t *bar, uint32_t parity) {
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+      if (!s_ok) return false;
+      if (global_timer_ns() - t0 > g.timeout_ns) {
+        atomicOr(g.status, kStatusWaitTimeout);
+        s_ok = 0;
+        return false;
+      }
+    }
+    return true;
+  };
+
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    uint32_t issued = 0;
+    for (uint32_t J = 0; J < g.G; ++J) {
+      if (!__all_sync(kFull, s_ok != 0)) break;
+      const uint32_t s = J % kStages;
+      const bool ok =
+          J < kStages || wait_bar(&empty[s], ((J / kStages) - 1) & 1);
+      if (!__all_sync(kFull, ok)) break;
+      issued = J + 1;
+      const uint64_t col0 = (uint64_t)J * g.g;
+      const uint32_t len = (uint32_t)min64(g.g, g.B - col0) * U;
+      const uint64_t r = stash_rows(J, g.g, g.A, g.B);
+      const char *st = g.stash + g.soff[J];
+      uint32_t bytes = 0;
+      for (uint32_t t = lane; t < Wc; t += 32) {
+        const uint64_t i = i0 + t;
+        const char *src = (i < r) ? st + i * g.g * U
+                                  : g.base + (i * g.B + col0) * U;
+        const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+        const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+        bytes += (uint32_t)(a1 - a0);
+        rowoff(s)[t] = t * g.pitch + (uint32_t)((uintptr_t)src - a0);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        bytes += __shfl_xor_sync(kFull, bytes, o);
+      // refuse (never issue) a bulk copy whose shared destination is not
+      // 16-byte aligned or would run past the stage
+      bool bad = ((smem_u32(stage(s)) & 15u) != 0) || (g.pitch & 15u) != 0 ||
+                 len + 32 > g.pitch;
+      if (__any_sync(kFull, bad)) {
+        if (lane == 0) {
+          atomicOr(g.status, kStatusBadLayout);
+          s_ok = 0;
+        }
+        break;
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
+      __syncwarp();
+      for (uint32_t t = lane; t < Wc; t += 32) {
+        const uint64_t i = i0 + t;
+        const char *src = (i < r) ? st + i * g.g * U
+                                  : g.base + (i * g.B + col0) * U;
+        const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+        const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+        bulk_g2s(stage(s) + (size_t)t * g.pitch, (const void *)a0,
+                 (uint32_t)(a1 - a0), &full[s]);
+      }
+    }
+    if (!s_ok) {
+      // after a failure: let this CTA's copies in flight land before exiting
+      const uint32_t j0 = issued > (uint32_t)kStages ? issued - kStages : 0;
+      for (uint32_t J = j0; J < issued; ++J) {
+        const uint64_t t0 = global_timer_ns();
+        while (!mbar_try_wait(&full[J % kStages], (J / kStages) & 1) &&
+               global_timer_ns() - t0 < g.timeout_ns) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- poller ----------------
+    for (uint32_t J = 0; J < g.G; ++J) {
+      const uint32_t s = J % kStages;
+      const bool landed = wait_bar(&full[s], (J / kStages) & 1);
+      if (!__all_sync(kFull, landed)) break;
+      if (lane == 0) st_release_gpu(g.progress + ch, J + 1);
+      const uint64_t col0 = (uint64_t)J * g.g;
+      const uint32_t gj = (uint32_t)min64(g.g, g.B - col0);
+      const uint64_t t0 = global_timer_ns();
+      bool good = true;
+      for (uint32_t kk = lane; kk < gj && good; kk += 32) {
+        const uint64_t lo = (col0 + kk) * g.A + i0;
+        const uint64_t hi = lo + Wc - 1;
+        const uint64_t c_lo = (lo / g.B) / g.W;
+        const uint64_t c_hi = min64((hi / g.B) / g.W, g.nchunks - 1);
+        for (uint64_t c = c_lo; c <= c_hi && good; ++c) {
+          if (c == ch) continue;
+          unsigned ns = 32;
+          while (ld_acquire_gpu(g.progress + c) < J + 1) {
+            if (!s_ok || global_timer_ns() - t0 > g.timeout_ns) {
+              good = false;
+              break;
+            }
+            __nanosleep(ns);
+            if (ns < 512) ns <<= 1;
+          }
+        }
+      }
+      if (__any_sync(kFull, !good)) {
+        if (lane == 0) {
+          atomicOr(g.status, kStatusWaitTimeout);
+          s_ok = 0;
+        }
+        break;
+      }
+      if (lane == 0) mbar_arrive(&ready[s]);
+    }
+    // never leave another CTA waiting on this one
+    if (!s_ok && lane == 0) st_release_gpu(g.progress + ch, g.G);
+  } else {
+    // ---------------- writers ----------------
+    const uint32_t wid = warp - 2;
+    const uint32_t wb = Wc * g.b;
+    T *dst = reinterpret_cast<T *>(g.base);
+    for (uint32_t J = 0; J < g.G; ++J) {
+      const uint32_t s = J % kStages;
+      const bool go = wait_bar(&ready[s], (J / kStages) & 1);
+      if (!__all_sync(kFull, go)) break;
+      const uint64_t col0 = (uint64_t)J * g.g;
+      const uint32_t gj = (uint32_t)min64(g.g, g.B - col0);
+      const unsigned char *tb = stage(s);
+      const uint32_t *ro = rowoff(s);
+      const uint64_t dbase = (col0 * g.A + i0) * g.b;
+      const uint64_t drow = g.A * g.b;
+      for (uint32_t kk = wid; kk < gj; kk += kWriterWarps) {
+        T *d = dst + dbase + kk * drow;
+        const uint32_t koff = kk * g.b * E;
+        if (g.b == 1) {
+#pragma unroll 4
+          for (uint32_t i = lane; i < Wc; i += 32)
+            __stcg(d + i, *reinterpret_cast<const T *>(tb + ro[i] + koff));
+        } else {
+          for (uint32_t rem = lane; rem < wb; rem += 32) {
+            const uint32_t i = fdiv(rem, g.div_b);
+            const uint32_t sub = rem - i * g.b;
+            __stcg(d + rem,
+                   *reinterpret_cast<const T *>(tb + ro[i] + koff + sub * E));
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+    }
+  }
+  __syncthreads();
+}
+
+// --- host side ---------------------------------------------------------------
+
+// Row pitch of a gathered strip: room for the 16-byte aligned superset a
+// bulk copy fetches, and an odd number of 16-byte words.
+static uint32_t stash_pitch(uint64_t row_bytes, int e) {
+  (void)e;
+  return (uint32_t)((row_bytes + 15) / 16 * 16 + 32);
+}
+
+template <int E>
+static int wave_occupancy(size_t smem) {
+  auto kern = k_stash_wave<E>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 0;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWaveThreads,
+                                                    smem) != cudaSuccess)
+    return 0;
+  return occ;
+}
+
+static int wave_occupancy_e(int e, size_t smem) {
+  switch (e) {
+    case 1: return wave_occupancy<1>(smem);
+    case 2: return wave_occupancy<2>(smem);
+    case 4: return wave_occupancy<4>(smem);
+    default: return wave_occupancy<8>(smem);
+  }
+}
+
+StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
+  StashPlan p;
+  if (e != 1 && e != 2 && e != 4 && e != 8) return p;
+  if (A < 2 || B < 2 || b == 0) return p;
+  const uint64_t U = (uint64_t)b * e;
+  const DeviceInfo &di = device_info();
+  const uint64_t max_smem = (uint64_t)di.max_smem_optin - 1024;
+  // aim for 512-byte strips; shrink the strip when the chunk would not fit.
+  // LM_STASH_STRIP / LM_STASH_PER_SM override the choice (tuning sweeps).
+  const char *es = getenv("LM_STASH_STRIP");
+  const char *ep = getenv("LM_STASH_PER_SM");
+  const uint64_t strips_default[3] = {512ull, 256ull, 128ull};
+  uint64_t strips[3] = {strips_default[0], strips_default[1], strips_default[2]};
+  if (es && atoll(es) > 0) strips[0] = strips[1] = strips[2] = (uint64_t)atoll(es);
+  const int per_sms[2] = {ep && atoi(ep) == 1 ? 1 : 2, 1};
+  for (uint64_t strip : strips) {
+    uint64_t g = std::max<uint64_t>(1, strip / U);
+    if (g > B) g = B;
+    const uint64_t G = (B + g - 1) / g;
+    const uint32_t pitch = stash_pitch(g * U, e);
+    for (int per_sm : per_sms) {
+      const uint64_t ctas = (uint64_t)di.sms * per_sm;
+      const uint64_t W = (A + ctas - 1) / ctas;
+      const uint64_t smem = (uint64_t)kStages * stash_stage_bytes(W, pitch);
+      if (smem > max_smem / per_sm) continue;
+      if (W * g * b >= 0xffffffffull || g * b >= 0xffffffffull) continue;
+      if (G > 65535) continue;  // K1 puts groups on grid.y
+      const uint64_t nch = (A + W - 1) / W;
+      if ((uint64_t)wave_occupancy_e(e, (size_t)smem) * di.sms < nch) continue;
+      p.feasible = true;
+      p.g = (uint32_t)g;
+      p.G = (uint32_t)G;
+      p.W = (uint32_t)W;
+      p.nchunks = (uint32_t)((A + W - 1) / W);
+      p.pitch = pitch;
+      p.smem_bytes = (size_t)smem;
+      p.ctas_per_sm = per_sm;
+      uint64_t total = 0;
+      for (uint64_t J = 0; J < G; ++J) total += stash_rows(J, g, A, B);
+      p.stash_bytes = (size_t)(total * g * U);
+      return p;
+    }
+  }
+  return p;
+}
+
+size_t stash_scratch_bytes(const StashPlan &p) {
+  // stash + offsets (G+1) + progress counters + status
+  return p.stash_bytes + 256 + (size_t)(p.G + 1) * 8 + 256 +
+         (size_t)p.nchunks * 4 + 256 + 4;
+}
+
+template <int E>
+static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
+  cudaError_t err;
+  {
+    ProfScope ps(s, "stash_offsets");
+    k_stash_offsets<<<1, 1024, 0, s>>>(const_cast<uint64_t *>(g.soff), g.A,
+                                       g.B, g.g, g.G, (uint64_t)g.g * g.b * E);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  {
+    const uint64_t rmax = stash_rows(g.G - 1, g.g, g.A, g.B);
+    if (rmax > 0) {
+      dim3 grid((unsigned)((rmax + kSaveRows - 1) / kSaveRows), g.G);
+      ProfScope ps(s, "stash_save");
+      k_stash_save<E><<<grid, kSaveThreads, 0, s>>>(g);
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+  }
+  auto kern = k_stash_wave<E>;
+  err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)p.smem_bytes);
+  if (err != cudaSuccess) return err;
+  int occ = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWaveThreads,
+                                                      p.smem_bytes);
+  if (err != cudaSuccess) return err;
+  const DeviceInfo &di = device_info();
+  if ((uint64_t)occ * di.sms < p.nchunks) return cudaErrorCooperativeLaunchTooLarge;
+  if (getenv("LM_VERBOSE"))
+    fprintf(stderr, "stash: g=%u G=%u W=%u chunks=%u smem=%zu occ=%d stash=%zu\n",
+            p.g, p.G, p.W, p.nchunks, p.smem_bytes, occ, p.stash_bytes);
+  void *args[] = {&g};
+  ProfScope ps(s, "stash_wave");
+  // cooperative launch: every CTA is co-resident, so the waits can end
+  err = cudaLaunchCooperativeKernel((const void *)kern, dim3(p.nchunks),
+                                    dim3(kWaveThreads), args, p.smem_bytes, s);
+  if (err != cudaSuccess) return err;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
+                            uint64_t B, uint32_t b, const StashPlan &p,
+                            void *scratch, uint32_t *status,
+                            uint64_t timeout_ns) {
+  if (!p.feasible) return cudaErrorInvalidValue;
+  char *sc = reinterpret_cast<char *>(scratch);
+  auto align = [](size_t v) { return (v + 255) / 256 * 256; };
+  StashArgs g;
+  g.base = reinterpret_cast<char *>(buf);
+  g.stash = sc;
+  size_t off = align(p.stash_bytes);
+  g.soff = reinterpret_cast<const uint64_t *>(sc + off);
+  off += align((size_t)(p.G + 1) * 8);
+  g.progress = reinterpret_cast<uint32_t *>(sc + off);
+  g.status = status;
+  g.A = A;
+  g.B = B;
+  g.b = b;
+  g.g = p.g;
+  g.G = p.G;
+  g.W = p.W;
+  g.nchunks = p.nchunks;
+  g.pitch = p.pitch;
+  g.gb = p.g * b;
+  g.div_gb = make_fastdiv(g.gb);
+  g.div_b = make_fastdiv(b);
+  g.timeout_ns = timeout_ns;
+  switch (e) {
+    case 1: return run_stash<1>(s, g, p);
+    case 2: return run_stash<2>(s, g, p);
+    case 4: return run_stash<4>(s, g, p);
+    case 8: return run_stash<8>(s, g, p);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace lm

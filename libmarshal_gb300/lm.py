@@ -53,6 +53,7 @@ _SIGS = {
     "lm_debug_pad_stall": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _LL,
                                 ctypes.c_ulonglong]),
     "lm_launch_count": (ctypes.c_ulonglong, []),
+    "lm_device_status": (ctypes.c_uint, [_VP]),
     "lm_prof_enable": (None, [_I]),
     "lm_prof_collect": (_I, [_VP, _I]),
     "gpu_aos_asta_bs_float": (_B, [_VP, _I, _I, _I, _VP]),

@@ -353,3 +353,71 @@ def test_elapsed_time_accumulates(L):
     assert L.lib().lm_transpose_100(None, d.data_ptr(), 4, 1024, 999, 1,
                                     ctypes.byref(et)) is False
     assert et.value > 5
+
+
+# ---- every plan of the 100 / 0100 planner ------------------------------------
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_every_method_on_medium_100(L, e):
+    # methods: 0 planner, 1 BS (may refuse), 2 PTTWAC, 3 stash, 4 two-pass
+    from libmarshal_gb300.lm import LMError
+    shapes = [(2048, 1031, 1), (1031, 2048, 1), (1500, 1200, 3),
+              (4096, 600, 2), (700, 3000, 1), (3000, 700, 5)]
+    for (A, B, b) in shapes:
+        src = O.random_bits(A * B * b, e, A * 7 + B)
+        want = O.t100(src, A, B, b)
+        for method in (0, 1, 2, 3, 4):
+            d = to_dev(src)
+            try:
+                L.transpose_0100(d, 1, A, B, b, method=method, elem_bytes=e)
+            except LMError:
+                assert method in (1, 3, 4), (A, B, b, e, method)
+                continue
+            assert np.array_equal(from_dev(d, e), want), (A, B, b, e, method)
+    assert L.lib().lm_device_status(None) == 0
+
+
+@pytest.mark.parametrize("e", [4, 8])
+def test_stash_plan_shapes(L, e):
+    # shapes with a partial last column group, few and many rows per chunk
+    rng = np.random.default_rng(e)
+    for _ in range(8):
+        A = int(rng.integers(300, 5000))
+        B = int(rng.integers(300, 5000))
+        b = int(rng.choice([1, 1, 2, 3, 7]))
+        if A * B * b * e > (64 << 20):
+            continue
+        src = O.random_bits(A * B * b, e, A + B)
+        d = to_dev(src)
+        L.transpose_0100(d, 1, A, B, b, method=3, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), O.t100(src, A, B, b)), (A, B, b)
+    assert L.lib().lm_device_status(None) == 0
+
+
+def _full_size_100(L, A, B, e, seed):
+    import torch
+    n = A * B
+    src = O.random_bits(n, e, seed)
+    want = np.empty_like(src)
+    O.lib().lmo_soa_asta_mt(src.ctypes.data, want.ctypes.data, B, A, 1, e,
+                            os.cpu_count() or 1)
+    d = to_dev(src)
+    L.transpose_100(d, A, B, 1, elem_bytes=e)
+    got = from_dev(d, e)
+    assert np.array_equal(got, want), (A, B, e)
+    # and back: the size-independent round-trip property
+    L.transpose_100(d, B, A, 1, elem_bytes=e)
+    assert np.array_equal(from_dev(d, e), src)
+    assert L.lib().lm_device_status(None) == 0
+    del d
+    torch.cuda.empty_cache()
+
+
+def test_headline_full_size_fp32(L):
+    # BASELINE headline: in-place 100 of the fp32 16384 x 12289 matrix
+    _full_size_100(L, 16384, 12289, 4, 2024)
+
+
+@pytest.mark.slow
+def test_large_fp64_32768x16000(L):
+    _full_size_100(L, 32768, 16000, 8, 2025)
