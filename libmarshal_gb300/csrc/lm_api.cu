@@ -98,6 +98,17 @@ struct Scratch {
   }
 };
 
+static bool get_scratch(Scratch &sc, size_t bytes, cudaStream_t s) {
+  pool_keep_memory();
+  sc.s = s;
+  cudaError_t e = cudaMallocAsync(&sc.p, bytes ? bytes : 4, s);
+  if (e != cudaSuccess) {
+    sc.p = nullptr;
+    return cuda_fail(e, "scratch allocation");
+  }
+  return false;
+}
+
 static bool get_zeroed(Scratch &sc, size_t bytes, cudaStream_t s) {
   pool_keep_memory();
   sc.s = s;
@@ -262,7 +273,10 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
     uint32_t *status = sp.feasible ? device_status_word() : nullptr;
     if (sp.feasible && status) {
       Scratch sc;
-      if (get_zeroed(sc, stash_scratch_bytes(sp), s)) return true;
+      if (get_scratch(sc, stash_scratch_bytes(sp), s)) return true;
+      cudaError_t ze = cudaMemsetAsync((char *)sc.p + stash_zero_offset(sp), 0,
+                                       stash_zero_bytes(sp), s);
+      if (ze != cudaSuccess) return cuda_fail(ze, "scratch clear");
       return check_launch(launch_stash100(s, buf, e, a, B, (uint32_t)b, sp,
                                           sc.p, status, wait_timeout_ns()),
                           "stash launch");

@@ -137,6 +137,21 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
                : "memory");
 }
 
+// 16-byte asynchronous copy global -> shared (both addresses 16-byte aligned).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)),
+               "l"(src)
+               : "memory");
+}
+
+// Arrives on `bar` once all of this thread's earlier cp.async copies have
+// completed (the barrier's expected count must include this arrival).
+__device__ __forceinline__ void cp_async_mbar_arrive_noinc(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
 // 1-D bulk copy global -> shared (the TMA engine); addresses and size must be
 // multiples of 16 bytes; completion is signalled on `bar` as transaction bytes.
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,

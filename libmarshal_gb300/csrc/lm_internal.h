@@ -88,7 +88,11 @@ struct StashPlan {
   size_t stash_bytes = 0;
 };
 StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e);
-size_t stash_scratch_bytes(const StashPlan &p);  // zeroed scratch to pass
+size_t stash_scratch_bytes(const StashPlan &p);  // scratch to pass
+// Byte range of that scratch that must be zero before the launch (the
+// progress counters); the rest is fully written before it is read.
+size_t stash_zero_offset(const StashPlan &p);
+size_t stash_zero_bytes(const StashPlan &p);
 cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
                             uint64_t B, uint32_t b, const StashPlan &p,
                             void *scratch, uint32_t *status,

@@ -52,6 +52,10 @@ struct StashArgs {
   FastDiv div_gb;
   FastDiv div_b;
   uint64_t timeout_ns;
+  uint32_t margin;       // stash margin k (steps of slack between CTAs)
+  uint32_t tma;          // 1: gather rows with bulk copies, 0: cp.async
+  uint64_t *trace;       // debug: per (chunk, step) timestamps, or null
+  uint32_t trace_ctas;
 };
 
 // Bytes of one ring stage: W rows of `pitch` bytes, then W uint32 row
@@ -62,24 +66,30 @@ __host__ __device__ __forceinline__ size_t stash_stage_bytes(uint64_t W,
   return (size_t)((W * pitch + W * 4 + 127) / 128 * 128);
 }
 
+// Rows whose group-J strip is saved: r(J) = ceil((g*A*(J+k) - g*J) / B), at
+// most A.  With margin k = 0 these are exactly the rows overwritten before
+// they are consumed; a margin k > 0 also saves the rows overwritten within k
+// steps after consumption (about k*g*A/B rows per step), so that a write of
+// step J depends only on gathers of steps <= J-k: the CTAs are no longer in
+// lockstep.
 __host__ __device__ __forceinline__ uint64_t stash_rows(uint64_t J, uint64_t g,
-                                                        uint64_t A,
-                                                        uint64_t B) {
-  // r(J) = ceil(g*J*(A-1)/B), at most A
-  const uint64_t num = g * J * (A - 1);
+                                                        uint64_t A, uint64_t B,
+                                                        uint64_t k) {
+  const uint64_t num = g * A * (J + k) - g * J;
   const uint64_t r = (num + B - 1) / B;
   return r < A ? r : A;
 }
 
 // K0: stash offsets (one thread per group, then a single-block scan).
 __global__ void k_stash_offsets(uint64_t *soff, uint64_t A, uint64_t B,
-                                uint32_t g, uint32_t G, uint64_t row_bytes) {
+                                uint32_t g, uint32_t G, uint64_t row_bytes,
+                                uint64_t k) {
   __shared__ uint64_t part[1024];
   const uint32_t t = threadIdx.x, nt = blockDim.x;
   const uint32_t per = (G + nt - 1) / nt;
   const uint32_t j0 = min(G, t * per), j1 = min(G, j0 + per);
   uint64_t s = 0;
-  for (uint32_t J = j0; J < j1; ++J) s += stash_rows(J, g, A, B) * row_bytes;
+  for (uint32_t J = j0; J < j1; ++J) s += stash_rows(J, g, A, B, k) * row_bytes;
   part[t] = s;
   __syncthreads();
   if (t == 0) {
@@ -95,7 +105,7 @@ __global__ void k_stash_offsets(uint64_t *soff, uint64_t A, uint64_t B,
   uint64_t acc = part[t];
   for (uint32_t J = j0; J < j1; ++J) {
     soff[J] = acc;
-    acc += stash_rows(J, g, A, B) * row_bytes;
+    acc += stash_rows(J, g, A, B, k) * row_bytes;
   }
 }
 
@@ -108,7 +118,7 @@ template <int E>
 __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
   using T = typename Elem<E>::T;
   const uint32_t J = blockIdx.y;
-  const uint64_t r = stash_rows(J, g.g, g.A, g.B);
+  const uint64_t r = stash_rows(J, g.g, g.A, g.B, g.margin);
   const uint64_t i0 = (uint64_t)blockIdx.x * kSaveRows;
   if (i0 >= r) return;
   const uint32_t nrows = (uint32_t)min64(kSaveRows, r - i0);
@@ -140,26 +150,37 @@ __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
 }
 
 // K2: the wavefront, warp-specialised.  Per CTA:
-//   warp 0 (producer): gathers step J into ring stage J % kStages with 1-D
-//     bulk copies (TMA), one per row, each a 16-byte aligned superset of the
-//     row strip (rowoff[] records where the strip starts);
-//   warp 1 (poller): when stage J has landed, publishes progress = J+1, then
+//   warps 0-3 (producers): gather step J into ring stage J % kStages with
+//     16-byte cp.async copies of a 16-byte aligned superset of every row
+//     strip (rowoff[] records where the strip starts); completion arrives on
+//     the stage's `full` barrier;
+//   warp 4 (poller): when stage J has landed, publishes progress = J+1, then
 //     waits for the CTAs whose rows hold original data in its destination
 //     range and releases the stage to the writers;
-//   warps 2.. (writers): write step J from the stage, then free it.
+//   warps 5.. (writers): write step J from the stage, then free it.
 // Stages are handed over with mbarriers (full / ready / empty); every wait is
 // bounded by %globaltimer; a timeout sets the status word and all roles stop.
 constexpr int kWaveThreads = 512;
 constexpr int kStages = 3;
-constexpr int kWriterWarps = kWaveThreads / 32 - 2;
+constexpr int kProducerWarps = 4;
+constexpr int kPublisherWarp = kProducerWarps;
+constexpr int kCheckerWarp = kProducerWarps + 1;
+constexpr int kWriterWarps = kWaveThreads / 32 - kProducerWarps - 2;
+constexpr uint32_t kCheckAhead = 4;  // steps whose chunks the checker prefetches
+constexpr int kMaxRowBlocks = 4;  // rows per chunk <= 128
+constexpr uint32_t kStashMargin = 3;
+constexpr uint32_t kMaxChunks = 1024;  // CTAs of the wave (co-resident)
+constexpr uint32_t kProgStride = 32;   // one 128-byte line per progress word
 
 template <int E>
 __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
   using T = typename Elem<E>::T;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[kStages], ready[kStages],
-      empty[kStages];
+      empty[kStages];  // ready = dependencies satisfied
   __shared__ volatile int s_ok;
+  __shared__ volatile int s_pstop;  // producers only: stop at this step
+  __shared__ uint32_t seen[kMaxChunks];  // poller: last progress read
   const uint32_t ch = blockIdx.x;
   const uint64_t i0 = (uint64_t)ch * g.W;
   if (i0 >= g.A) return;
@@ -175,13 +196,15 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
   };
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full[s], 1);
+      mbar_init(&full[s], g.tma ? 1u : kProducerWarps * 32u);
       mbar_init(&ready[s], 1);
       mbar_init(&empty[s], kWriterWarps);
     }
     fence_mbar_init();
     s_ok = 1;
+    s_pstop = 0;
   }
+  for (uint32_t c = threadIdx.x; c < kMaxChunks; c += blockDim.x) seen[c] = 0;
   __syncthreads();
 
   // bounded wait; false on timeout or when another role has failed
@@ -198,116 +221,188 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     return true;
   };
 
-  if (warp == 0) {
-    // ---------------- producer ----------------
+  if (warp < kProducerWarps) {
+    // ---------------- producers ----------------
+    const uint32_t pt = threadIdx.x;  // 0 .. 127
+    constexpr uint32_t kP = kProducerWarps * 32;
     uint32_t issued = 0;
     for (uint32_t J = 0; J < g.G; ++J) {
-      if (!__all_sync(kFull, s_ok != 0)) break;
       const uint32_t s = J % kStages;
-      const bool ok =
-          J < kStages || wait_bar(&empty[s], ((J / kStages) - 1) & 1);
-      if (!__all_sync(kFull, ok)) break;
+      bool stop = !s_ok;
+      if (!stop && J >= kStages)
+        stop = !wait_bar(&empty[s], ((J / kStages) - 1) & 1);
+      // the four producer warps take the same decision: s_pstop is written
+      // only before the first barrier and read only between the two
+      if (stop) s_pstop = 1;
+      asm volatile("bar.sync 1, %0;" ::"n"(kP) : "memory");
+      const bool stop_all = s_pstop != 0;
+      asm volatile("bar.sync 1, %0;" ::"n"(kP) : "memory");
+      if (stop_all) {
+        s_ok = 0;
+        break;
+      }
       issued = J + 1;
       const uint64_t col0 = (uint64_t)J * g.g;
       const uint32_t len = (uint32_t)min64(g.g, g.B - col0) * U;
-      const uint64_t r = stash_rows(J, g.g, g.A, g.B);
+      const uint64_t r = stash_rows(J, g.g, g.A, g.B, g.margin);
       const char *st = g.stash + g.soff[J];
-      uint32_t bytes = 0;
-      for (uint32_t t = lane; t < Wc; t += 32) {
-        const uint64_t i = i0 + t;
-        const char *src = (i < r) ? st + i * g.g * U
-                                  : g.base + (i * g.B + col0) * U;
-        const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
-        const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
-        bytes += (uint32_t)(a1 - a0);
-        rowoff(s)[t] = t * g.pitch + (uint32_t)((uintptr_t)src - a0);
-      }
+      unsigned char *sb = stage(s);
+      if (g.tma) {
+        // warp 0: one bulk copy per row (16-byte aligned superset)
+        if (warp == 0) {
+          uint32_t bytes = 0;
+          for (uint32_t t = lane; t < Wc; t += 32) {
+            const uint64_t i = i0 + t;
+            const char *src = (i < r) ? st + i * g.g * U
+                                      : g.base + (i * g.B + col0) * U;
+            const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+            const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+            bytes += (uint32_t)(a1 - a0);
+            rowoff(s)[t] = t * g.pitch + (uint32_t)((uintptr_t)src - a0);
+          }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-        bytes += __shfl_xor_sync(kFull, bytes, o);
-      // refuse (never issue) a bulk copy whose shared destination is not
-      // 16-byte aligned or would run past the stage
-      bool bad = ((smem_u32(stage(s)) & 15u) != 0) || (g.pitch & 15u) != 0 ||
-                 len + 32 > g.pitch;
-      if (__any_sync(kFull, bad)) {
-        if (lane == 0) {
-          atomicOr(g.status, kStatusBadLayout);
-          s_ok = 0;
+          for (int o = 16; o > 0; o >>= 1)
+            bytes += __shfl_xor_sync(kFull, bytes, o);
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (g.trace && ch < g.trace_ctas && lane == 0)
+            g.trace[((uint64_t)ch * g.G + J) * 4 + 0] = global_timer_ns();
+          if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
+          __syncwarp();
+          for (uint32_t t = lane; t < Wc; t += 32) {
+            const uint64_t i = i0 + t;
+            const char *src = (i < r) ? st + i * g.g * U
+                                      : g.base + (i * g.B + col0) * U;
+            const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+            const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+            bulk_g2s(sb + (size_t)t * g.pitch, (const void *)a0,
+                     (uint32_t)(a1 - a0), &full[s]);
+          }
         }
-        break;
-      }
-      fence_proxy_async_smem();
-      __syncwarp();
-      if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
-      __syncwarp();
-      for (uint32_t t = lane; t < Wc; t += 32) {
-        const uint64_t i = i0 + t;
-        const char *src = (i < r) ? st + i * g.g * U
-                                  : g.base + (i * g.B + col0) * U;
-        const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
-        const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
-        bulk_g2s(stage(s) + (size_t)t * g.pitch, (const void *)a0,
-                 (uint32_t)(a1 - a0), &full[s]);
+      } else {
+        // 16-byte chunks per row (upper bound; chunks past the strip skipped)
+        const uint32_t nc = (len + 15) / 16 + 1;
+        for (uint32_t w = pt; w < Wc * nc; w += kP) {
+          const uint32_t t = w / nc, c = w - t * nc;
+          const uint64_t i = i0 + t;
+          const char *src = (i < r) ? st + i * g.g * U
+                                    : g.base + (i * g.B + col0) * U;
+          const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+          const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+          if (c == 0)
+            rowoff(s)[t] = t * g.pitch + (uint32_t)((uintptr_t)src - a0);
+          if (a0 + 16 * (uintptr_t)c < a1)
+            cp_async16(sb + (size_t)t * g.pitch + 16 * c,
+                       (const void *)(a0 + 16 * (uintptr_t)c));
+        }
+        if (g.trace && ch < g.trace_ctas && pt == 0)
+          g.trace[((uint64_t)ch * g.G + J) * 4 + 0] = global_timer_ns();
+        cp_async_mbar_arrive_noinc(&full[s]);
       }
     }
     if (!s_ok) {
       // after a failure: let this CTA's copies in flight land before exiting
-      const uint32_t j0 = issued > (uint32_t)kStages ? issued - kStages : 0;
-      for (uint32_t J = j0; J < issued; ++J) {
-        const uint64_t t0 = global_timer_ns();
-        while (!mbar_try_wait(&full[J % kStages], (J / kStages) & 1) &&
-               global_timer_ns() - t0 < g.timeout_ns) {
+      if (g.tma) {
+        const uint32_t j0 = issued > (uint32_t)kStages ? issued - kStages : 0;
+        for (uint32_t J = j0; J < issued; ++J) {
+          const uint64_t t0 = global_timer_ns();
+          while (!mbar_try_wait(&full[J % kStages], (J / kStages) & 1) &&
+                 global_timer_ns() - t0 < g.timeout_ns) {
+          }
         }
+      } else {
+        asm volatile("cp.async.wait_all;" ::: "memory");
       }
     }
-  } else if (warp == 1) {
-    // ---------------- poller ----------------
+  } else if (warp == kPublisherWarp) {
+    // ---------------- publisher: progress = steps gathered ----------------
     for (uint32_t J = 0; J < g.G; ++J) {
       const uint32_t s = J % kStages;
       const bool landed = wait_bar(&full[s], (J / kStages) & 1);
       if (!__all_sync(kFull, landed)) break;
-      if (lane == 0) st_release_gpu(g.progress + ch, J + 1);
-      const uint64_t col0 = (uint64_t)J * g.g;
-      const uint32_t gj = (uint32_t)min64(g.g, g.B - col0);
-      const uint64_t t0 = global_timer_ns();
-      bool good = true;
-      for (uint32_t kk = lane; kk < gj && good; kk += 32) {
-        const uint64_t lo = (col0 + kk) * g.A + i0;
-        const uint64_t hi = lo + Wc - 1;
-        const uint64_t c_lo = (lo / g.B) / g.W;
-        const uint64_t c_hi = min64((hi / g.B) / g.W, g.nchunks - 1);
-        for (uint64_t c = c_lo; c <= c_hi && good; ++c) {
-          if (c == ch) continue;
-          unsigned ns = 32;
-          while (ld_acquire_gpu(g.progress + c) < J + 1) {
-            if (!s_ok || global_timer_ns() - t0 > g.timeout_ns) {
-              good = false;
-              break;
-            }
-            __nanosleep(ns);
-            if (ns < 512) ns <<= 1;
-          }
-        }
-      }
-      if (__any_sync(kFull, !good)) {
-        if (lane == 0) {
-          atomicOr(g.status, kStatusWaitTimeout);
-          s_ok = 0;
-        }
-        break;
-      }
-      if (lane == 0) mbar_arrive(&ready[s]);
+      if (lane == 0) st_release_gpu(g.progress + kProgStride * ch, J + 1);
+      if (g.trace && ch < g.trace_ctas && lane == 0)
+        g.trace[((uint64_t)ch * g.G + J) * 4 + 1] = global_timer_ns();
     }
     // never leave another CTA waiting on this one
-    if (!s_ok && lane == 0) st_release_gpu(g.progress + ch, g.G);
+    if (!s_ok && lane == 0) st_release_gpu(g.progress + kProgStride * ch, g.G);
+  } else if (warp == kCheckerWarp) {
+    // ---------------- checker: dependencies of each step ----------------
+    // The rows holding original data in step J's destination range lie in
+    // chunks [first(J), last(J)] (a superset); J needs their progress >=
+    // J+1-margin.  seen[] caches the last value read (progress only grows),
+    // and the chunks of the next kCheckAhead steps are read along, so most
+    // steps are decided from the cache.
+    auto first_c = [&](uint64_t J) {
+      return ((J * g.g * g.A + i0) / g.B) / g.W;
+    };
+    auto last_c = [&](uint64_t J) {
+      const uint64_t c0 = J * g.g;
+      const uint64_t gj = min64(g.g, g.B - c0);
+      return min64((((c0 + gj - 1) * g.A + i0 + Wc - 1) / g.B) / g.W,
+                   g.nchunks - 1);
+    };
+    bool good = true;
+    for (uint32_t J = 0; J < g.G && good; ++J) {
+      const uint32_t s = J % kStages;
+      const uint32_t need = J + 1 > g.margin ? J + 1 - g.margin : 0u;
+      if (need > 0) {
+        const uint64_t cf = first_c(J), cl = last_c(J);
+        const uint64_t la = last_c(min64(J + kCheckAhead, g.G - 1));
+        bool loaded = false;
+        const uint64_t t0 = global_timer_ns();
+        for (uint64_t c = cf + lane; c <= la && good; c += 32) {
+          if (c == ch) continue;
+          if (c <= cl) {
+            if (seen[c] >= need) continue;
+            unsigned ns = 32;
+            uint32_t v;
+            while ((v = ld_relaxed_gpu(g.progress + kProgStride * c)) < need) {
+              if (!s_ok || global_timer_ns() - t0 > g.timeout_ns) {
+                good = false;
+                break;
+              }
+              __nanosleep(ns);
+              if (ns < 256) ns <<= 1;
+            }
+            seen[c] = v;
+            loaded = true;
+          } else if (seen[c] < need + kCheckAhead) {
+            seen[c] = ld_relaxed_gpu(g.progress + kProgStride * c);
+            loaded = true;
+          }
+        }
+        good = __all_sync(kFull, good);
+        // relaxed reads followed by this fence act as acquire for every
+        // later access of this CTA (the writers' stores come after it)
+        if (__any_sync(kFull, loaded))
+          asm volatile("fence.acq_rel.gpu;" ::: "memory");
+      }
+      if (!good) break;
+      if (J >= kStages) {
+        const bool ok = wait_bar(&empty[s], ((J / kStages) - 1) & 1);
+        if (!__all_sync(kFull, ok)) {
+          good = false;
+          break;
+        }
+      }
+      if (g.trace && ch < g.trace_ctas && lane == 0)
+        g.trace[((uint64_t)ch * g.G + J) * 4 + 2] = global_timer_ns();
+      if (lane == 0) mbar_arrive(&ready[s]);
+    }
+    if (!good && lane == 0) {
+      atomicOr(g.status, kStatusWaitTimeout);
+      s_ok = 0;
+    }
   } else {
     // ---------------- writers ----------------
-    const uint32_t wid = warp - 2;
+    const uint32_t wid = warp - kProducerWarps - 2;
     const uint32_t wb = Wc * g.b;
     T *dst = reinterpret_cast<T *>(g.base);
     for (uint32_t J = 0; J < g.G; ++J) {
       const uint32_t s = J % kStages;
-      const bool go = wait_bar(&ready[s], (J / kStages) & 1);
+      const bool go = wait_bar(&full[s], (J / kStages) & 1) &&
+                      wait_bar(&ready[s], (J / kStages) & 1);
       if (!__all_sync(kFull, go)) break;
       const uint64_t col0 = (uint64_t)J * g.g;
       const uint32_t gj = (uint32_t)min64(g.g, g.B - col0);
@@ -315,14 +410,28 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
       const uint32_t *ro = rowoff(s);
       const uint64_t dbase = (col0 * g.A + i0) * g.b;
       const uint64_t drow = g.A * g.b;
-      for (uint32_t kk = wid; kk < gj; kk += kWriterWarps) {
-        T *d = dst + dbase + kk * drow;
-        const uint32_t koff = kk * g.b * E;
-        if (g.b == 1) {
-#pragma unroll 4
-          for (uint32_t i = lane; i < Wc; i += 32)
-            __stcg(d + i, *reinterpret_cast<const T *>(tb + ro[i] + koff));
-        } else {
+      if (g.b == 1) {
+        // each lane's rows i = lane + 32m: offsets once per step
+        uint32_t rof[kMaxRowBlocks];
+#pragma unroll
+        for (int m = 0; m < kMaxRowBlocks; ++m) {
+          const uint32_t i = lane + 32 * m;
+          rof[m] = i < Wc ? ro[i] : 0u;
+        }
+        for (uint32_t kk = wid; kk < gj; kk += kWriterWarps) {
+          T *d = dst + dbase + kk * drow;
+          const uint32_t koff = kk * E;
+#pragma unroll
+          for (int m = 0; m < kMaxRowBlocks; ++m) {
+            const uint32_t i = lane + 32 * m;
+            if (i < Wc)
+              __stcg(d + i, *reinterpret_cast<const T *>(tb + rof[m] + koff));
+          }
+        }
+      } else {
+        for (uint32_t kk = wid; kk < gj; kk += kWriterWarps) {
+          T *d = dst + dbase + kk * drow;
+          const uint32_t koff = kk * g.b * E;
           for (uint32_t rem = lane; rem < wb; rem += 32) {
             const uint32_t i = fdiv(rem, g.div_b);
             const uint32_t sub = rem - i * g.b;
@@ -332,6 +441,8 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
         }
       }
       __syncwarp();
+      if (g.trace && ch < g.trace_ctas && wid == 0 && lane == 0)
+        g.trace[((uint64_t)ch * g.G + J) * 4 + 3] = global_timer_ns();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
   }
@@ -396,6 +507,8 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
       if (smem > max_smem / per_sm) continue;
       if (W * g * b >= 0xffffffffull || g * b >= 0xffffffffull) continue;
       if (G > 65535) continue;  // K1 puts groups on grid.y
+      if (W > 32u * kMaxRowBlocks) continue;
+      if ((A + W - 1) / W > kMaxChunks) continue;
       const uint64_t nch = (A + W - 1) / W;
       if ((uint64_t)wave_occupancy_e(e, (size_t)smem) * di.sms < nch) continue;
       p.feasible = true;
@@ -407,7 +520,8 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
       p.smem_bytes = (size_t)smem;
       p.ctas_per_sm = per_sm;
       uint64_t total = 0;
-      for (uint64_t J = 0; J < G; ++J) total += stash_rows(J, g, A, B);
+      for (uint64_t J = 0; J < G; ++J)
+        total += stash_rows(J, g, A, B, kStashMargin);
       p.stash_bytes = (size_t)(total * g * U);
       return p;
     }
@@ -415,10 +529,20 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
   return p;
 }
 
+static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+size_t stash_zero_offset(const StashPlan &p) {
+  return align256(p.stash_bytes) + align256((size_t)(p.G + 1) * 8);
+}
+
+size_t stash_zero_bytes(const StashPlan &p) {
+  return (size_t)p.nchunks * 4 * kProgStride;
+}
+
 size_t stash_scratch_bytes(const StashPlan &p) {
   // stash + offsets (G+1) + progress counters + status
   return p.stash_bytes + 256 + (size_t)(p.G + 1) * 8 + 256 +
-         (size_t)p.nchunks * 4 + 256 + 4;
+         (size_t)p.nchunks * 4 * kProgStride + 256 + 4;
 }
 
 template <int E>
@@ -427,11 +551,12 @@ static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   {
     ProfScope ps(s, "stash_offsets");
     k_stash_offsets<<<1, 1024, 0, s>>>(const_cast<uint64_t *>(g.soff), g.A,
-                                       g.B, g.g, g.G, (uint64_t)g.g * g.b * E);
+                                       g.B, g.g, g.G, (uint64_t)g.g * g.b * E,
+                                       g.margin);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
   {
-    const uint64_t rmax = stash_rows(g.G - 1, g.g, g.A, g.B);
+    const uint64_t rmax = stash_rows(g.G - 1, g.g, g.A, g.B, g.margin);
     if (rmax > 0) {
       dim3 grid((unsigned)((rmax + kSaveRows - 1) / kSaveRows), g.G);
       ProfScope ps(s, "stash_save");
@@ -452,12 +577,48 @@ static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   if (getenv("LM_VERBOSE"))
     fprintf(stderr, "stash: g=%u G=%u W=%u chunks=%u smem=%zu occ=%d stash=%zu\n",
             p.g, p.G, p.W, p.nchunks, p.smem_bytes, occ, p.stash_bytes);
+  // LM_STASH_TRACE=n: record step timestamps of the first n CTAs and print
+  // a summary (debugging aid; allocates and synchronises).
+  const char *tr = getenv("LM_STASH_TRACE");
+  uint64_t *trace = nullptr;
+  if (tr && atoi(tr) > 0) {
+    g.trace_ctas = (uint32_t)std::min(atoi(tr), (int)p.nchunks);
+    const size_t tb = (size_t)g.trace_ctas * g.G * 4 * 8;
+    if (cudaMalloc(&trace, tb) == cudaSuccess) {
+      cudaMemsetAsync(trace, 0, tb, s);
+      g.trace = trace;
+    }
+  }
   void *args[] = {&g};
   ProfScope ps(s, "stash_wave");
   // cooperative launch: every CTA is co-resident, so the waits can end
   err = cudaLaunchCooperativeKernel((const void *)kern, dim3(p.nchunks),
                                     dim3(kWaveThreads), args, p.smem_bytes, s);
   if (err != cudaSuccess) return err;
+  if (trace) {
+    cudaStreamSynchronize(s);
+    const size_t n = (size_t)g.trace_ctas * g.G * 4;
+    uint64_t *h = (uint64_t *)malloc(n * 8);
+    cudaMemcpy(h, trace, n * 8, cudaMemcpyDeviceToHost);
+    for (uint32_t c = 0; c < g.trace_ctas; ++c) {
+      double land = 0, deps = 0, wr = 0, per = 0;
+      uint64_t *t = h + (size_t)c * g.G * 4;
+      for (uint32_t J = 1; J + 1 < g.G; ++J) {
+        auto d = [](uint64_t a, uint64_t b) { return (double)(int64_t)(a - b); };
+        land += d(t[J * 4 + 1], t[J * 4 + 0]);
+        deps += d(t[J * 4 + 2], t[J * 4 + 1]);
+        wr += d(t[J * 4 + 3], std::max(t[J * 4 + 2], t[J * 4 + 1]));
+        per += d(t[(J + 1) * 4 + 3], t[J * 4 + 3]);
+      }
+      const double k = (double)(g.G - 2) * 1000.0;
+      fprintf(stderr, "stash trace cta %u: issue->published %.2f us, published->deps ok %.2f us, "
+              "ready->written %.2f us, step period %.2f us, total %.1f us\n", c, land / k,
+              deps / k, wr / k, per / k,
+              (double)(t[(g.G - 1) * 4 + 3] - t[0]) / 1000.0);
+    }
+    free(h);
+    cudaFree(trace);
+  }
   return cudaGetLastError();
 }
 
@@ -488,6 +649,13 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   g.div_gb = make_fastdiv(g.gb);
   g.div_b = make_fastdiv(b);
   g.timeout_ns = timeout_ns;
+  g.trace = nullptr;
+  g.trace_ctas = 0;
+  g.margin = kStashMargin;
+  {
+    const char *gm = getenv("LM_STASH_GATHER");
+    g.tma = (gm && gm[0] == 'c') ? 0u : 1u;  // "cpasync" selects cp.async
+  }
   switch (e) {
     case 1: return run_stash<1>(s, g, p);
     case 2: return run_stash<2>(s, g, p);
