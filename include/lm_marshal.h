@@ -152,6 +152,60 @@ bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
                         int x_size, int y_size, int pad_size, int unpad,
                         long long stall_block, unsigned long long timeout_ns);
 
+/* ---- batched conversion (no reference counterpart) -------------------------
+ * A batch is a list of independent in-place jobs, each on its own device
+ * buffer (buffers must not overlap), of any op and element width.
+ * lm_batch_run plans the list: jobs whose tiles fit one CTA's shared memory
+ * become work items of one persistent work-stealing kernel (mixed widths);
+ * jobs whose tiles fit the shared memory of a thread-block cluster become
+ * items of a persistent clustered kernel (one launch per cluster size; not
+ * with LM_BATCH_NO_CLUSTER); jobs that fit the batch's scratch arena
+ * (LM_BATCH_SCRATCH_MB, default 1024; not with LM_BATCH_NO_SCRATCH) are
+ * staged: transposed block by block into the arena, then copied back, in
+ * waves of at most one arena each (two launches per wave, at most 8 waves);
+ * the rest go through the per-op planner, spread over the batch's side
+ * streams, whose algorithm choice per shape class is autotuned (timed once
+ * on a scratch buffer, then remembered; LM_TUNE_FILE persists the table).  With LM_BATCH_GRAPH, the second run of an identical
+ * job list is captured into a CUDA graph and later runs replay it.  Ordered
+ * on `stream` as a whole. */
+enum {
+  LM_OP_0100 = 0,      /* d0..d3 = A, a, B, b:  [A][a][B][b] -> [A][B][a][b] */
+  LM_OP_010 = 1,       /* A, a, B:              [A][a][B] -> [A][B][a] */
+  LM_OP_100 = 2,       /* A, B, b:              [A][B][b] -> [B][A][b] */
+  LM_OP_AOS_ASTA = 3,  /* height, width, tile:  [h][w] -> [h/t][w][t] */
+  LM_OP_ASTA_AOS = 4,  /* height, width, tile:  [h/t][w][t] -> [h][w] */
+  LM_OP_SOA_ASTA = 5,  /* height, width, tile:  [w][h] -> [h/t][w][t] */
+  LM_OP_ASTA_SOA = 6,  /* height, width, tile:  [h/t][w][t] -> [w][h] */
+  LM_OP_TRANSPOSE = 7  /* M, N:                 [M][N] -> [N][M] */
+};
+enum {
+  LM_BATCH_GRAPH = 1,
+  LM_BATCH_NO_TUNE = 2,
+  LM_BATCH_NO_CLUSTER = 4,
+  LM_BATCH_NO_SCRATCH = 8 /* strictly in place: no staged form */
+};
+typedef struct {
+  void *buf;      /* device buffer, converted in place */
+  int elem_bytes; /* 1, 2, 4 or 8 */
+  int op;         /* LM_OP_* */
+  long long d0, d1, d2, d3;
+} lm_job;
+typedef struct {
+  unsigned long long bytes, small_bytes, big_bytes, large_bytes;
+  unsigned long long small_jobs, big_jobs, large_jobs, identity;
+  unsigned long long small_items, big_items;
+  unsigned long long band_bytes, band_jobs, band_items;
+  unsigned long long staged_bytes, staged_jobs, staged_waves;
+} lm_batch_stats;
+typedef struct lm_batch_st *lm_batch_t;
+bool lm_batch_create(lm_batch_t *out);
+void lm_batch_destroy(lm_batch_t batch);
+bool lm_batch_run(lm_batch_t batch, lm_stream_t stream, const lm_job *jobs,
+                  int njobs, unsigned flags);
+bool lm_batch_stats_get(lm_batch_t batch, lm_batch_stats *out);
+/* Autotuner table: entries tuned so far (and loaded from LM_TUNE_FILE). */
+int lm_tune_entries(void);
+
 /* ---- profiling (counterpart of include/cl_profile.h:6-63) ----------------
  * lm_launch_count: kernels launched by this library since it was loaded.
  * lm_prof_enable(1): from now on every launch is bracketed by a CUDA event

@@ -16,8 +16,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 
 #include "lm_core.cuh"
 #include "lm_internal.h"
@@ -187,6 +189,11 @@ struct OpTimer {
 
 static bool valid_e(int e) { return e == 1 || e == 2 || e == 4 || e == 8; }
 
+// Elements are moved as e-byte words, so the buffer must be e-byte aligned.
+static bool misaligned(const void *buf, int e) {
+  return ((uintptr_t)buf & (uintptr_t)(e - 1)) != 0;
+}
+
 // Limit for every inter-CTA wait (LM_WAIT_TIMEOUT_MS overrides, default 2 s).
 static uint64_t wait_timeout_ns() {
   const char *v = getenv("LM_WAIT_TIMEOUT_MS");
@@ -251,6 +258,7 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   if (T == 0 || a == 0 || B == 0 || b == 0) return false;  // empty
   if (a == 1 || B == 1) return false;                      // identity
   if (buf == nullptr) return fail("null buffer");
+  if (misaligned(buf, e)) return fail("buffer must be aligned to the element size");
   if (a * B >= 0xffffffffull) return fail("a*B must be < 2^32");
   if (m == Method::Auto || m == Method::BS) {
     BsPlan p = plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e);
@@ -306,11 +314,143 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   return run_pttwac_direct(s, buf, e, T, a, B, b);
 }
 
+// ---- autotuner ----------------------------------------------------------------
+// Shape class = (element bytes, log2 of a, B and b, and whether the op has
+// several instances).  For each class met by a tuned call the candidate plans
+// are timed once on a scratch buffer of the job's size and the fastest is
+// remembered; LM_TUNE_FILE names a text file that is loaded at first use and
+// appended to ("e la lB lb multi method" per line).
+
+struct TuneKey {
+  int e, la, lB, lb, multi;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(e, la, lB, lb, multi) <
+           std::tie(o.e, o.la, o.lB, o.lb, o.multi);
+  }
+};
+
+static int ilog2(uint64_t v) {
+  int l = 0;
+  while (v > 1) {
+    v >>= 1;
+    ++l;
+  }
+  return l;
+}
+
+static std::mutex g_tune_mu;
+static std::map<TuneKey, int> g_tune;
+static bool g_tune_loaded = false;
+
+static void tune_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char *f = getenv("LM_TUNE_FILE");
+  if (!f) return;
+  FILE *fp = fopen(f, "r");
+  if (!fp) return;
+  TuneKey k;
+  int m;
+  while (fscanf(fp, "%d %d %d %d %d %d", &k.e, &k.la, &k.lB, &k.lb, &k.multi,
+                &m) == 6)
+    g_tune[k] = m;
+  fclose(fp);
+}
+
+static void tune_save_locked(const TuneKey &k, int m) {
+  const char *f = getenv("LM_TUNE_FILE");
+  if (!f) return;
+  FILE *fp = fopen(f, "a");
+  if (!fp) return;
+  fprintf(fp, "%d %d %d %d %d %d\n", k.e, k.la, k.lB, k.lb, k.multi, m);
+  fclose(fp);
+}
+
+// Whether a forced method applies to this exact shape (a tuned choice is
+// shared by every shape of its class, whose factors may differ).
+static bool method_applies(Method m, int e, uint64_t T, uint64_t a,
+                           uint64_t B, uint64_t b) {
+  switch (m) {
+    case Method::Stash:
+      return T == 1 && plan_stash(a, B, (uint32_t)b, e).feasible;
+    case Method::TwoPass:
+      return b * e < 128 && (split_a(a, B, b, e) || split_B(a, B, b, e));
+    case Method::BS:
+      return plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e).feasible;
+    default:
+      return true;
+  }
+}
+
+static Method tuned_method(cudaStream_t s, int e, uint64_t T, uint64_t a,
+                           uint64_t B, uint64_t b) {
+  const TuneKey key{e, ilog2(a), ilog2(B), ilog2(b), T > 1 ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return (Method)it->second;
+  }
+  const uint64_t bytes = T * a * B * b * (uint64_t)e;
+  Method cand[4];
+  int nc = 0;
+  cand[nc++] = Method::Auto;
+  if (T == 1 && plan_stash(a, B, (uint32_t)b, e).feasible) cand[nc++] = Method::Stash;
+  if (b * e < 128 && (split_a(a, B, b, e) || split_B(a, B, b, e)))
+    cand[nc++] = Method::TwoPass;
+  cand[nc++] = Method::Pttwac;
+  void *tmp = nullptr;
+  Method best = Method::Auto;
+  if (cudaMallocAsync(&tmp, bytes, s) == cudaSuccess) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = 1e30f;
+    for (int i = 0; i < nc; ++i) {
+      const std::string saved = g_err;
+      if (!method_applies(cand[i], e, T, a, B, b) ||
+          do_0100(s, tmp, e, T, a, B, b, cand[i])) {  // warm-up
+        g_err = saved;
+        continue;
+      }
+      cudaEventRecord(e0, s);
+      do_0100(s, tmp, e, T, a, B, b, cand[i]);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = cand[i];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(tmp, s);
+  }
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune[key] = (int)best;
+  tune_save_locked(key, (int)best);
+  return best;
+}
+
+bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
+                      uint64_t a, uint64_t B, uint64_t b, int tune) {
+  Method m = Method::Auto;
+  if (tune && valid_e(e) && T > 0 && a > 1 && B > 1 && b > 0 &&
+      T * a * B * b * (uint64_t)e >= (1ull << 20)) {
+    m = tuned_method(s, e, T, a, B, b);
+    if (!method_applies(m, e, T, a, B, b)) m = Method::Auto;
+  }
+  return do_0100(s, buf, e, T, a, B, b, m);
+}
+
 static bool do_010_pttwac(cudaStream_t s, void *buf, int e, uint64_t A,
                           uint64_t a, uint64_t B, int R, int P) {
   if (!valid_e(e)) return fail("element size must be 1, 2, 4 or 8 (got %d)", e);
   if (A == 0 || a <= 1 || B <= 1) return false;
   if (buf == nullptr) return fail("null buffer");
+  if (misaligned(buf, e)) return fail("buffer must be aligned to the element size");
   if (R < 1 || R > 32 || (R & (R - 1))) return fail("R must be a power of two in [1, 32]");
   if (P < 0) return fail("P must be >= 0");
   if (a * B < 0xffffffffull && pttwac010_smem_fits((uint32_t)a, (uint32_t)B, R, P))
@@ -328,6 +468,7 @@ static bool do_pad(cudaStream_t s, void *buf, int e, int64_t x, int64_t y,
   if (x < 0 || y < 0 || pad < x) return fail("padding needs 0 <= x <= pad, y >= 0");
   if ((y == 0 || pad == x) && stall_block < 0) return false;
   if (buf == nullptr) return fail("null buffer");
+  if (misaligned(buf, e)) return fail("buffer must be aligned to the element size");
   Scratch sc, st;
   if (get_zeroed(sc, pad_scratch_bytes(x, y, pad), s)) return true;
   if (get_zeroed(st, 4, s)) return true;
@@ -559,6 +700,12 @@ unsigned lm_device_status(lm_stream_t stream) {
     return 0xffffffffu;
   if (v) cudaMemsetAsync(w, 0, 4, s);
   return v;
+}
+
+int lm_tune_entries(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  tune_load_locked();
+  return (int)g_tune.size();
 }
 
 // Planner query used by the Python API's IsFeasible(): 1 when the 0100 tile

@@ -1,0 +1,1154 @@
+// lm_batch.cu -- many independent conversions in few launches.
+//
+// No reference counterpart: the reference converts one buffer per call and
+// tunes work-group sizes by hand per shape (src/cl_marshal.cc:165-241,
+// 388-465).  Here a batch of jobs (each one in-place 0100 on its own buffer,
+// any element width) is split in two:
+//  * jobs whose tiles fit one CTA's shared memory become work items of ONE
+//    persistent kernel: every CTA claims items from an atomic counter (work
+//    stealing) and runs the barrier-synchronised tile transposition on them,
+//    whatever their element width; two such kernels run, one for items of at
+//    most kSmallItem bytes (several CTAs per SM) and one for large tiles (one
+//    CTA per SM);
+//  * the remaining (large) jobs go through the per-op planner, each on the
+//    batch's stream.
+// The job table and the item list are uploaded once per batch from pinned
+// host memory; lm_batch_run can record the whole batch into a CUDA graph and
+// replay it for an identical job list.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+#include <cooperative_groups.h>
+
+#include "lm_core.cuh"
+#include "lm_internal.h"
+#include "../../include/lm_marshal.h"
+
+namespace lm {
+
+constexpr int kBatchThreads = 512;
+constexpr uint32_t kSmallItem = 40 * 1024;
+constexpr int kBandGroups = 4;       // clusters of 2, 4, 8 and 16 CTAs
+constexpr int kMaxWaves = 8;         // staged waves per batch
+constexpr int kCounterStride = 32;   // counters 128 bytes apart
+// small, big, one per cluster size, two per staged wave
+constexpr size_t kCounterBytes =
+    (size_t)(2 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
+constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
+constexpr int kSideStreams = 4;      // streams the large jobs spread over
+
+struct BJob {
+  char *base;
+  uint32_t e;
+  uint32_t a, B, b;
+  uint32_t row_elems, aB, tile_elems, pitch;
+  FastDiv div_row, div_b, div_aB, div_a;
+  uint32_t band;  // cluster form: units per CTA band (pitch = band pitch)
+  // staged form: S x S unit blocks, nI x nJ of them per tile, written
+  // transposed to `scratch` and copied back
+  char *scratch;
+  uint32_t S, nJ, nIJ;
+  FastDiv div_Sb, div_nJ, div_nIJ;
+  uint64_t bytes;
+};
+
+struct BItem {
+  uint32_t job;
+  uint32_t ntiles;
+  uint64_t tile0;
+};
+
+struct BatchArgs {
+  const BJob *jobs;
+  const BItem *items;
+  uint32_t nitems;
+  uint32_t *counter;
+  uint32_t *status;  // set to kStatusWaitTimeout if a staged load never lands
+};
+
+template <int E>
+__device__ void batch_item(const BJob &j, const BItem &it, unsigned char *smem) {
+  using T = typename Elem<E>::T;
+  const uint32_t rows = it.ntiles * j.a;
+  const uint32_t n = rows * j.row_elems;
+  const uint64_t e0 = it.tile0 * (uint64_t)j.tile_elems;
+  T *buf = reinterpret_cast<T *>(j.base) + e0;
+  // load: contiguous elements -> padded shared rows
+  for (uint32_t base = threadIdx.x; base < n; base += kBatchThreads * 4) {
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t idx = base + u * kBatchThreads;
+      if (idx < n) v[u] = __ldcg(buf + idx);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t idx = base + u * kBatchThreads;
+      if (idx < n) {
+        const uint32_t row = fdiv(idx, j.div_row);
+        const uint32_t col = idx - row * j.row_elems;
+        *reinterpret_cast<T *>(smem + row * j.pitch + col * E) = v[u];
+      }
+    }
+  }
+  __syncthreads();
+  // store: output o <- (tile t, j, i, sub)
+  for (uint32_t base = threadIdx.x; base < n; base += kBatchThreads * 4) {
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t o = base + u * kBatchThreads;
+      if (o < n) {
+        uint32_t unit = o, sub = 0;
+        if (j.b != 1) {
+          unit = fdiv(o, j.div_b);
+          sub = o - unit * j.b;
+        }
+        const uint32_t t = fdiv(unit, j.div_aB);
+        const uint32_t u2 = unit - t * j.aB;
+        const uint32_t jj = fdiv(u2, j.div_a);
+        const uint32_t i = u2 - jj * j.a;
+        v[u] = *reinterpret_cast<const T *>(smem + (t * j.a + i) * j.pitch +
+                                            (jj * j.b + sub) * E);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t o = base + u * kBatchThreads;
+      if (o < n) __stcg(buf + o, v[u]);
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBatchThreads) k_batch_bs(BatchArgs g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_item;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
+    __syncthreads();
+    const uint32_t k = s_item;
+    __syncthreads();
+    if (k >= g.nitems) break;
+    const BItem it = g.items[k];
+    const BJob j = g.jobs[it.job];
+    switch (j.e) {
+      case 1: batch_item<1>(j, it, smem); break;
+      case 2: batch_item<2>(j, it, smem); break;
+      case 4: batch_item<4>(j, it, smem); break;
+      default: batch_item<8>(j, it, smem); break;
+    }
+  }
+}
+
+// Tiles larger than one CTA's shared memory, processed by persistent
+// clusters: rank 0 claims the next item and shares it through distributed
+// shared memory; each CTA stages a column band of the tile with bulk copies
+// (16-byte aligned supersets of the row segments) and writes the output rows
+// of its band from its own shared memory.
+constexpr uint32_t kBandMaxRows = 1024;
+namespace cgb = cooperative_groups;
+
+template <int E>
+__device__ void band_item(const BJob &j, uint64_t tile, uint32_t rank,
+                          unsigned char *smem, uint32_t *rowoff,
+                          uint64_t *bar, uint32_t &parity, int *s_ok,
+                          uint32_t *status, cgb::cluster_group &cl) {
+  using T = typename Elem<E>::T;
+  const uint32_t bc0 = min(j.B, rank * j.band);
+  const uint32_t bc1 = min(j.B, bc0 + j.band);
+  const uint32_t band_elems = (bc1 - bc0) * j.b;
+  // after a load that never landed this CTA stages nothing more (its shared
+  // memory may still be written) but keeps joining the cluster barriers
+  const uint32_t len = *s_ok ? band_elems * E : 0;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T *t = reinterpret_cast<T *>(j.base) + tile * (uint64_t)j.tile_elems;
+  if (warp == 0 && len > 0) {
+    uint32_t bytes = 0;
+    for (uint32_t r = lane; r < j.a; r += 32) {
+      const char *src = reinterpret_cast<const char *>(
+          t + (uint64_t)r * j.row_elems + (uint64_t)bc0 * j.b);
+      const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+      const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+      bytes += (uint32_t)(a1 - a0);
+      rowoff[r] = r * j.pitch + (uint32_t)((uintptr_t)src - a0);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+    fence_proxy_async_smem();
+    if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+    __syncwarp();
+    for (uint32_t r = lane; r < j.a; r += 32) {
+      const char *src = reinterpret_cast<const char *>(
+          t + (uint64_t)r * j.row_elems + (uint64_t)bc0 * j.b);
+      const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+      const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+      bulk_g2s(smem + (size_t)r * j.pitch, (const void *)a0,
+               (uint32_t)(a1 - a0), bar);
+    }
+  }
+  if (len > 0) {
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(bar, parity))
+      if (global_timer_ns() - t0 > 2000000000ull) {
+        *s_ok = 0;  // every thread of the CTA times out alike
+        if (threadIdx.x == 0) atomicExch(status, kStatusWaitTimeout);
+        break;
+      }
+    parity ^= 1;
+  }
+  cl.sync();  // every band of this tile staged before any output is written
+  const uint32_t n = j.a * band_elems;
+  T *dst = t + (uint64_t)bc0 * j.a * j.b;
+  if (len > 0 && *s_ok) {
+    for (uint32_t base = threadIdx.x; base < n; base += kBatchThreads * 4) {
+      T v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t o = base + u * kBatchThreads;
+        if (o < n) {
+          uint32_t unit = o, sub = 0;
+          if (j.b != 1) {
+            unit = fdiv(o, j.div_b);
+            sub = o - unit * j.b;
+          }
+          const uint32_t jj = fdiv(unit, j.div_a);
+          const uint32_t i = unit - jj * j.a;
+          v[u] = *reinterpret_cast<const T *>(smem + rowoff[i] +
+                                              (jj * j.b + sub) * E);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t o = base + u * kBatchThreads;
+        if (o < n) __stcg(dst + o, v[u]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBatchThreads) k_batch_band(BatchArgs g) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t rowoff[kBandMaxRows];
+  __shared__ uint32_t s_item;
+  __shared__ int s_ok;
+  cgb::cluster_group cl = cgb::this_cluster();
+  const uint32_t rank = cl.block_rank();
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    s_ok = 1;
+  }
+  uint32_t *item0 = cl.map_shared_rank(&s_item, 0);
+  uint32_t parity = 0;
+  while (true) {
+    if (rank == 0 && threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
+    cl.sync();  // rank 0's claim is visible; also orders the mbarrier init
+    const uint32_t k = *item0;
+    if (k >= g.nitems) break;
+    const BItem it = g.items[k];
+    const BJob j = g.jobs[it.job];
+    switch (j.e) {
+      case 1: band_item<1>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
+      case 2: band_item<2>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
+      case 4: band_item<4>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
+      default: band_item<8>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
+    }
+  }
+  cl.sync();  // nobody leaves while rank 0's s_item may still be read
+}
+
+// Staged form, for tiles too large for any on-chip plan: each S x S block of
+// units of a tile is transposed through shared memory into the batch's
+// scratch arena (out of place, so blocks need no ordering), then a second
+// kernel copies the arena back over the job's buffer.  Items are runs of
+// blocks (gather) or of 16-byte vectors (copy back).
+constexpr int kStageThreads = 256;
+constexpr uint32_t kStageTileBytes = 32 * 1024;  // S*S*b*e at most
+constexpr uint32_t kStageBlocksPerItem = 16;
+constexpr uint64_t kCopyVecsPerItem = 16384;     // 256 KB
+
+template <int E>
+__device__ void gather_block(const BJob &j, uint32_t q, unsigned char *smem) {
+  using T = typename Elem<E>::T;
+  const uint32_t t = fdiv(q, j.div_nIJ);
+  const uint32_t r = q - t * j.nIJ;
+  const uint32_t bi = fdiv(r, j.div_nJ);
+  const uint32_t bj = r - bi * j.nJ;
+  const uint32_t i0 = bi * j.S, j0 = bj * j.S;
+  const uint32_t si = min(j.S, j.a - i0), sj = min(j.S, j.B - j0);
+  const uint32_t Sb = j.S * j.b;
+  const uint32_t n = j.S * Sb;  // a full block; edge blocks skip the rest
+  const T *src = reinterpret_cast<const T *>(j.base) +
+                 (uint64_t)t * j.tile_elems + (uint64_t)i0 * j.row_elems +
+                 (uint64_t)j0 * j.b;
+  T *dst = reinterpret_cast<T *>(j.scratch) + (uint64_t)t * j.tile_elems +
+           ((uint64_t)j0 * j.a + i0) * j.b;
+  const uint32_t lim_c = sj * j.b, lim_o = si * j.b;
+  for (uint32_t base = threadIdx.x; base < n; base += kStageThreads * 4) {
+    T v[4];
+    uint32_t sm[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t idx = base + u * kStageThreads;
+      const uint32_t rr = fdiv(idx, j.div_Sb);
+      const uint32_t c = idx - rr * Sb;
+      sm[u] = 0xffffffffu;
+      if (idx < n && rr < si && c < lim_c) {
+        v[u] = __ldcs(src + (uint64_t)rr * j.row_elems + c);
+        sm[u] = rr * j.pitch + c * E;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (sm[u] != 0xffffffffu) *reinterpret_cast<T *>(smem + sm[u]) = v[u];
+  }
+  __syncthreads();
+  for (uint32_t base = threadIdx.x; base < n; base += kStageThreads * 4) {
+    T v[4];
+    uint64_t go[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t idx = base + u * kStageThreads;
+      const uint32_t jj = fdiv(idx, j.div_Sb);
+      const uint32_t rem = idx - jj * Sb;
+      go[u] = ~0ull;
+      if (idx < n && jj < sj && rem < lim_o) {
+        uint32_t ii = rem, sub = 0;
+        if (j.b != 1) {
+          ii = fdiv(rem, j.div_b);
+          sub = rem - ii * j.b;
+        }
+        v[u] = *reinterpret_cast<const T *>(smem + ii * j.pitch +
+                                            (jj * j.b + sub) * E);
+        go[u] = (uint64_t)jj * j.a * j.b + rem;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (go[u] != ~0ull) __stcg(dst + go[u], v[u]);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kStageThreads) k_batch_gather(BatchArgs g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_item;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
+    __syncthreads();
+    const uint32_t k = s_item;
+    __syncthreads();
+    if (k >= g.nitems) break;
+    const BItem it = g.items[k];
+    const BJob j = g.jobs[it.job];
+    for (uint32_t q = (uint32_t)it.tile0; q < (uint32_t)it.tile0 + it.ntiles; ++q) {
+      switch (j.e) {
+        case 1: gather_block<1>(j, q, smem); break;
+        case 2: gather_block<2>(j, q, smem); break;
+        case 4: gather_block<4>(j, q, smem); break;
+        default: gather_block<8>(j, q, smem); break;
+      }
+    }
+  }
+}
+
+// Copy back: the arena copy of a job starts at the same address modulo 16 as
+// the job's buffer, so one run of 16-byte vectors serves both; item 0 of a
+// job also copies the ragged head and tail bytes.
+__global__ void __launch_bounds__(kStageThreads) k_batch_copyback(BatchArgs g) {
+  __shared__ uint32_t s_item;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
+    __syncthreads();
+    const uint32_t k = s_item;
+    __syncthreads();
+    if (k >= g.nitems) break;
+    const BItem it = g.items[k];
+    const BJob j = g.jobs[it.job];
+    const uintptr_t d = (uintptr_t)j.base;
+    const uint64_t head = min64((16 - (d & 15)) & 15, j.bytes);
+    const uint64_t nvec = (j.bytes - head) / 16;
+    const uint4 *vs = reinterpret_cast<const uint4 *>(j.scratch + head);
+    uint4 *vd = reinterpret_cast<uint4 *>(j.base + head);
+    const uint64_t v1 = min64(it.tile0 + kCopyVecsPerItem, nvec);
+    for (uint64_t v = it.tile0 + threadIdx.x; v < v1; v += kStageThreads)
+      __stcs(vd + v, __ldcs(vs + v));
+    if (it.tile0 == 0) {
+      const uint64_t tail0 = head + nvec * 16;
+      for (uint64_t x = threadIdx.x; x < head + (j.bytes - tail0);
+           x += kStageThreads) {
+        const uint64_t off = x < head ? x : tail0 + (x - head);
+        j.base[off] = j.scratch[off];
+      }
+    }
+  }
+}
+
+// ---- host -------------------------------------------------------------------
+
+// Cluster form of one tile of a x (B*b) elements of e bytes: the smallest
+// cluster (2..16 CTAs) whose column bands fit `budget` bytes of shared memory
+// each, preferring bands small enough for two CTAs per SM and clusters of at
+// most 8.  Returns the group index (log2(C) - 1) or -1.
+static int band_group(uint64_t a, uint64_t B, uint64_t b, int e, size_t budget,
+                      uint32_t *band, uint32_t *pitch) {
+  if (a > kBandMaxRows || a * B * b >= 0xffffffffull) return -1;
+  const size_t half = budget / 2 - 1024;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int gi = 0; gi < kBandGroups; ++gi) {
+      const uint64_t C = 2ull << gi;
+      if (pass == 0 && C > 8) break;
+      const uint64_t bd = (B + C - 1) / C;
+      // a 16-byte aligned superset of a row segment of len bytes spans at
+      // most round16(len) + 16 bytes
+      const uint64_t bp = (bd * b * e + 15) / 16 * 16 + 16;
+      if (bp * a <= (pass == 0 ? half : budget)) {
+        *band = (uint32_t)bd;
+        *pitch = (uint32_t)bp;
+        return gi;
+      }
+    }
+  }
+  return -1;
+}
+
+static uint32_t batch_pitch(uint64_t row_bytes, int e) {
+  const uint64_t g = e == 8 ? 8 : 4;
+  uint64_t p = (row_bytes + g - 1) / g * g;
+  if (((p / g) & 1) == 0) p += g;
+  return (uint32_t)p;
+}
+
+struct Normalized {
+  bool ok = false;
+  uint64_t T = 0, a = 0, B = 0, b = 0;
+};
+
+// Every op of the library as a 0100(T, a, B, b).
+static Normalized normalize(const lm_job &jb) {
+  Normalized n;
+  const int64_t d0 = jb.d0, d1 = jb.d1, d2 = jb.d2, d3 = jb.d3;
+  switch (jb.op) {
+    case LM_OP_0100:  // A a B b
+      if (d0 < 0 || d1 < 0 || d2 < 0 || d3 < 0) return n;
+      n.T = d0; n.a = d1; n.B = d2; n.b = d3;
+      break;
+    case LM_OP_010:  // A a B
+      if (d0 < 0 || d1 < 0 || d2 < 0) return n;
+      n.T = d0; n.a = d1; n.B = d2; n.b = 1;
+      break;
+    case LM_OP_100:  // A B b
+      if (d0 < 0 || d1 < 0 || d2 < 0) return n;
+      n.T = 1; n.a = d0; n.B = d1; n.b = d2;
+      break;
+    case LM_OP_AOS_ASTA:  // height width tile
+      if (d2 <= 0 || d0 < 0 || d1 < 0 || d0 % d2) return n;
+      n.T = d0 / d2; n.a = d2; n.B = d1; n.b = 1;
+      break;
+    case LM_OP_ASTA_AOS:  // height width tile: [h/t][w][t] -> [h][w]
+      if (d2 <= 0 || d0 < 0 || d1 < 0 || d0 % d2) return n;
+      n.T = d0 / d2; n.a = d1; n.B = d2; n.b = 1;
+      break;
+    case LM_OP_SOA_ASTA:  // height width tile: [w][h] -> [h/t][w][t]
+      if (d2 <= 0 || d0 < 0 || d1 < 0 || d0 % d2) return n;
+      n.T = 1; n.a = d1; n.B = d0 / d2; n.b = d2;
+      break;
+    case LM_OP_ASTA_SOA:  // height width tile: [h/t][w][t] -> [w][h]
+      if (d2 <= 0 || d0 < 0 || d1 < 0 || d0 % d2) return n;
+      n.T = 1; n.a = d0 / d2; n.B = d1; n.b = d2;
+      break;
+    case LM_OP_TRANSPOSE:  // M N
+      if (d0 < 0 || d1 < 0) return n;
+      n.T = 1; n.a = d0; n.B = d1; n.b = 1;
+      break;
+    default:
+      return n;
+  }
+  n.ok = true;
+  return n;
+}
+
+}  // namespace lm
+
+struct lm_batch_st {
+  std::vector<lm::BJob> jobs;
+  std::vector<lm::BItem> small, big;
+  std::vector<lm::BItem> band[lm::kBandGroups];  // cluster of 2 << g CTAs
+  size_t band_smem[lm::kBandGroups] = {};
+  // staged waves: gather items, copy-back items, shared memory of the gather
+  std::vector<lm::BItem> wgather[lm::kMaxWaves], wcopy[lm::kMaxWaves];
+  size_t wsmem[lm::kMaxWaves] = {};
+  int nwaves = 0;
+  char *d_arena = nullptr;  // scratch of the staged jobs of one wave
+  uint64_t cap_arena = 0, need_arena = 0;
+  std::vector<uint32_t> large;  // indices of jobs run by the planner
+  std::vector<lm::Normalized> norm;
+  // device side
+  lm::BJob *d_jobs = nullptr;
+  lm::BItem *d_items = nullptr;
+  uint32_t *d_counters = nullptr;
+  size_t cap_jobs = 0, cap_items = 0;
+  // pinned staging
+  void *h_stage = nullptr;
+  size_t cap_stage = 0;
+  // graph cache
+  cudaGraphExec_t gexec = nullptr;
+  uint64_t gkey = 0;
+  void *h_gstage = nullptr;  // pinned copy of the job table owned by gexec
+  cudaEvent_t uploaded = nullptr;  // last upload from h_stage
+  cudaStream_t side[lm::kSideStreams] = {};  // large jobs run here
+  cudaEvent_t join[lm::kSideStreams] = {};
+  cudaEvent_t fork = nullptr;
+  uint64_t seen_key = 0;  // job list of the previous graph-mode run
+  // last run statistics
+  lm_batch_stats stats;
+  int device = -1;
+};
+
+using namespace lm;
+
+static uint64_t hash_jobs(const lm_job *jobs, int n) {
+  uint64_t h = 1469598103934665603ull;
+  const unsigned char *p = reinterpret_cast<const unsigned char *>(jobs);
+  for (size_t i = 0; i < (size_t)n * sizeof(lm_job); ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h ^ (uint64_t)n;
+}
+
+// A captured graph holds the device addresses of the tables and the arena:
+// any reallocation retires it.
+static void drop_graph(lm_batch_t bt) {
+  if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
+  bt->gexec = nullptr;
+  bt->gkey = 0;
+}
+
+static bool grow(lm_batch_t bt, size_t njobs, size_t nitems) {
+  if (bt->need_arena > bt->cap_arena) {
+    drop_graph(bt);
+    if (bt->d_arena) cudaFree(bt->d_arena);
+    bt->d_arena = nullptr;
+    bt->cap_arena = 0;
+    if (cudaMalloc(&bt->d_arena, bt->need_arena) != cudaSuccess) {
+      bt->d_arena = nullptr;
+      return set_error("batch: cannot allocate the staging arena");
+    }
+    bt->cap_arena = bt->need_arena;
+  }
+  if (njobs > bt->cap_jobs) {
+    drop_graph(bt);
+    if (bt->d_jobs) cudaFree(bt->d_jobs);
+    bt->cap_jobs = std::max<size_t>(njobs, 2 * bt->cap_jobs);
+    if (cudaMalloc(&bt->d_jobs, bt->cap_jobs * sizeof(BJob)) != cudaSuccess) {
+      bt->d_jobs = nullptr;
+      bt->cap_jobs = 0;
+      return set_error("batch: cannot allocate the job table");
+    }
+  }
+  if (nitems > bt->cap_items) {
+    drop_graph(bt);
+    if (bt->d_items) cudaFree(bt->d_items);
+    bt->cap_items = std::max<size_t>(nitems, 2 * bt->cap_items);
+    if (cudaMalloc(&bt->d_items, bt->cap_items * sizeof(BItem)) != cudaSuccess) {
+      bt->d_items = nullptr;
+      bt->cap_items = 0;
+      return set_error("batch: cannot allocate the item list");
+    }
+  }
+  if (!bt->d_counters) {
+    if (cudaMalloc(&bt->d_counters, kCounterBytes) != cudaSuccess)
+      return set_error("batch: cannot allocate counters");
+  }
+  const size_t stage = njobs * sizeof(BJob) + nitems * sizeof(BItem) + 256;
+  if (stage > bt->cap_stage) {
+    if (bt->uploaded) cudaEventSynchronize(bt->uploaded);
+    if (bt->h_stage) cudaFreeHost(bt->h_stage);
+    bt->cap_stage = std::max(stage, 2 * bt->cap_stage);
+    if (cudaMallocHost(&bt->h_stage, bt->cap_stage) != cudaSuccess) {
+      bt->h_stage = nullptr;
+      bt->cap_stage = 0;
+      return set_error("batch: cannot allocate the pinned staging buffer");
+    }
+  }
+  return false;
+}
+
+// Bytes of scratch the staged jobs of one wave may use (LM_BATCH_SCRATCH_MB
+// overrides the default of 1 GiB; 0 turns the staged form off).
+static uint64_t arena_bytes() {
+  const char *v = getenv("LM_BATCH_SCRATCH_MB");
+  if (v && *v) return (uint64_t)strtoull(v, nullptr, 10) << 20;
+  return kDefaultArenaBytes;
+}
+
+static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
+                     uint32_t pitch) {
+  j.base = (char *)jb.buf;
+  j.e = jb.elem_bytes;
+  j.a = (uint32_t)nz.a;
+  j.B = (uint32_t)nz.B;
+  j.b = (uint32_t)nz.b;
+  j.row_elems = (uint32_t)(nz.B * nz.b);
+  j.aB = (uint32_t)(nz.a * nz.B);
+  j.tile_elems = (uint32_t)(nz.a * nz.B * nz.b);
+  j.pitch = pitch;
+  j.div_row = make_fastdiv(j.row_elems);
+  j.div_b = make_fastdiv(j.b);
+  j.div_aB = make_fastdiv(j.aB);
+  j.div_a = make_fastdiv(j.a);
+  j.band = 0;
+  j.scratch = nullptr;
+  j.S = j.nJ = j.nIJ = 0;
+  j.bytes = 0;
+}
+
+// Host planning of a job list into small items, big items, cluster items and
+// large jobs.
+static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
+                       unsigned flags) {
+  const DeviceInfo &di = device_info();
+  const uint64_t max_tile = (uint64_t)di.max_smem_optin - 1024;
+  // dynamic shared memory left to the cluster kernel beside its row table
+  const size_t band_budget =
+      (size_t)di.max_smem_optin - (kBandMaxRows * 4 + 512);
+  bt->jobs.clear();
+  bt->small.clear();
+  bt->big.clear();
+  for (int gi = 0; gi < kBandGroups; ++gi) {
+    bt->band[gi].clear();
+    bt->band_smem[gi] = 0;
+  }
+  bt->large.clear();
+  for (int w = 0; w < kMaxWaves; ++w) {
+    bt->wgather[w].clear();
+    bt->wcopy[w].clear();
+    bt->wsmem[w] = 0;
+  }
+  bt->nwaves = 0;
+  bt->need_arena = 0;
+  uint64_t wave_used = 0;
+  const uint64_t arena_cap = (flags & LM_BATCH_NO_SCRATCH) ? 0 : arena_bytes();
+  bt->norm.assign(n, Normalized());
+  memset(&bt->stats, 0, sizeof(bt->stats));
+  for (int k = 0; k < n; ++k) {
+    const lm_job &jb = jobs[k];
+    if (jb.elem_bytes != 1 && jb.elem_bytes != 2 && jb.elem_bytes != 4 &&
+        jb.elem_bytes != 8) {
+      char m[128];
+      snprintf(m, sizeof(m), "batch: job %d: element size must be 1/2/4/8", k);
+      return set_error(m);
+    }
+    Normalized nz = normalize(jb);
+    if (!nz.ok) {
+      char m[128];
+      snprintf(m, sizeof(m), "batch: job %d: bad op or dimensions", k);
+      return set_error(m);
+    }
+    bt->norm[k] = nz;
+    const uint64_t bytes = nz.T * nz.a * nz.B * nz.b * (uint64_t)jb.elem_bytes;
+    bt->stats.bytes += bytes;
+    if (nz.T == 0 || nz.a <= 1 || nz.B <= 1 || nz.b == 0) {
+      bt->stats.identity += 1;  // nothing to move
+      continue;
+    }
+    if (jb.buf == nullptr) {
+      char m[128];
+      snprintf(m, sizeof(m), "batch: job %d: null buffer", k);
+      return set_error(m);
+    }
+    if ((uintptr_t)jb.buf % (uintptr_t)jb.elem_bytes) {
+      char m[128];
+      snprintf(m, sizeof(m),
+               "batch: job %d: buffer must be aligned to the element size", k);
+      return set_error(m);
+    }
+    const uint64_t row_elems = nz.B * nz.b;
+    const uint64_t tile_elems = row_elems * nz.a;
+    const uint32_t pitch = batch_pitch(row_elems * jb.elem_bytes, jb.elem_bytes);
+    const uint64_t tile_smem = (uint64_t)pitch * nz.a;
+    if (tile_elems >= 0xffffffffull || tile_smem > max_tile) {
+      uint32_t band = 0, bpitch = 0;
+      const int gi = (flags & LM_BATCH_NO_CLUSTER)
+                         ? -1
+                         : band_group(nz.a, nz.B, nz.b, jb.elem_bytes,
+                                      band_budget, &band, &bpitch);
+      if (gi >= 0) {
+        BJob j;
+        fill_job(j, jb, nz, bpitch);
+        j.band = band;
+        const uint32_t jid = (uint32_t)bt->jobs.size();
+        bt->jobs.push_back(j);
+        for (uint64_t t0 = 0; t0 < nz.T; ++t0) {
+          BItem it;
+          it.job = jid;
+          it.tile0 = t0;
+          it.ntiles = 1;
+          bt->band[gi].push_back(it);
+        }
+        bt->band_smem[gi] =
+            std::max<size_t>(bt->band_smem[gi], (size_t)bpitch * nz.a);
+        bt->stats.band_jobs += 1;
+        bt->stats.band_bytes += bytes;
+        continue;
+      }
+      // staged: the job fits the arena (in the current wave or a new one)
+      const uint64_t unit = nz.b * (uint64_t)jb.elem_bytes;
+      const uint64_t foot = (bytes + 255) / 256 * 256 + 256;
+      if (foot <= arena_cap && unit <= kStageTileBytes &&
+          tile_elems < 0xffffffffull) {
+        if (bt->nwaves == 0 || wave_used + foot > arena_cap) {
+          if (bt->nwaves == kMaxWaves) goto planner;
+          bt->nwaves += 1;
+          wave_used = 0;
+        }
+        {
+          const int w = bt->nwaves - 1;
+          uint32_t S = 128;
+          while (S > 1 && (uint64_t)S * S * unit > kStageTileBytes) S >>= 1;
+          const uint64_t nI = (nz.a + S - 1) / S, nJ = (nz.B + S - 1) / S;
+          if (nz.T * nI * nJ >= 0xffffffffull) goto planner;
+          BJob j;
+          const uint32_t sp = batch_pitch((uint64_t)S * unit, jb.elem_bytes);
+          fill_job(j, jb, nz, sp);
+          j.S = S;
+          j.nJ = (uint32_t)nJ;
+          j.nIJ = (uint32_t)(nI * nJ);
+          j.div_Sb = make_fastdiv(S * (uint32_t)nz.b);
+          j.div_nJ = make_fastdiv(j.nJ);
+          j.div_nIJ = make_fastdiv(j.nIJ);
+          j.bytes = bytes;
+          // same address modulo 16 as the buffer (see k_batch_copyback);
+          // the arena base is set when the wave is enqueued
+          j.scratch = (char *)(uintptr_t)(wave_used + ((uintptr_t)jb.buf & 15));
+          const uint32_t jid = (uint32_t)bt->jobs.size();
+          bt->jobs.push_back(j);
+          const uint64_t nblk = nz.T * nI * nJ;
+          for (uint64_t q = 0; q < nblk; q += kStageBlocksPerItem) {
+            BItem it;
+            it.job = jid;
+            it.tile0 = q;
+            it.ntiles = (uint32_t)std::min<uint64_t>(kStageBlocksPerItem, nblk - q);
+            bt->wgather[w].push_back(it);
+          }
+          const uint64_t nvec = bytes / 16 + 1;
+          for (uint64_t v = 0; v < nvec; v += kCopyVecsPerItem) {
+            BItem it;
+            it.job = jid;
+            it.tile0 = v;
+            it.ntiles = 0;
+            bt->wcopy[w].push_back(it);
+          }
+          bt->wsmem[w] = std::max<size_t>(bt->wsmem[w], (size_t)S * sp);
+          wave_used += foot;
+          bt->need_arena = std::max(bt->need_arena, wave_used);
+          bt->stats.staged_jobs += 1;
+          bt->stats.staged_bytes += bytes;
+          continue;
+        }
+      }
+    planner:
+      bt->large.push_back((uint32_t)k);
+      bt->stats.large_jobs += 1;
+      bt->stats.large_bytes += bytes;
+      continue;
+    }
+    BJob j;
+    fill_job(j, jb, nz, pitch);
+    const uint32_t jid = (uint32_t)bt->jobs.size();
+    bt->jobs.push_back(j);
+    if (tile_smem <= kSmallItem) {
+      uint64_t k_t = std::max<uint64_t>(1, kSmallItem / tile_smem);
+      while (k_t > 1 && k_t * tile_elems >= 0xffffffffull) --k_t;
+      for (uint64_t t0 = 0; t0 < nz.T; t0 += k_t) {
+        BItem it;
+        it.job = jid;
+        it.tile0 = t0;
+        it.ntiles = (uint32_t)std::min<uint64_t>(k_t, nz.T - t0);
+        bt->small.push_back(it);
+      }
+      bt->stats.small_jobs += 1;
+      bt->stats.small_bytes += bytes;
+    } else {
+      for (uint64_t t0 = 0; t0 < nz.T; ++t0) {
+        BItem it;
+        it.job = jid;
+        it.tile0 = t0;
+        it.ntiles = 1;
+        bt->big.push_back(it);
+      }
+      bt->stats.big_jobs += 1;
+      bt->stats.big_bytes += bytes;
+    }
+  }
+  bt->stats.small_items = bt->small.size();
+  bt->stats.big_items = bt->big.size();
+  for (int gi = 0; gi < kBandGroups; ++gi)
+    bt->stats.band_items += bt->band[gi].size();
+  bt->stats.staged_waves = bt->nwaves;
+  return false;
+}
+
+static bool launch_band(cudaStream_t s, const BJob *d_jobs,
+                        const BItem *d_items, uint32_t nitems,
+                        uint32_t *counter, size_t smem, int C) {
+  if (nitems == 0) return false;
+  cudaError_t err = cudaFuncSetAttribute(
+      k_batch_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err == cudaSuccess && C > 8)
+    err = cudaFuncSetAttribute(k_batch_band,
+                               cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (err != cudaSuccess) return set_error("batch: cluster kernel attributes");
+  const DeviceInfo &di = device_info();
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kBatchThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)(C * std::max(1, di.sms / C)));
+  int max_clusters = 0;
+  err = cudaOccupancyMaxActiveClusters(&max_clusters, k_batch_band, &cfg);
+  if (err != cudaSuccess || max_clusters < 1)
+    return set_error("batch: no cluster fits the device");
+  const uint64_t ncl = std::min<uint64_t>((uint64_t)max_clusters, nitems);
+  cfg.gridDim = dim3((unsigned)(ncl * C));
+  BatchArgs g;
+  g.jobs = d_jobs;
+  g.items = d_items;
+  g.nitems = nitems;
+  g.counter = counter;
+  g.status = device_status_word();
+  if (getenv("LM_VERBOSE"))
+    fprintf(stderr, "batch_band: C=%d smem=%zu items=%u clusters=%llu\n", C,
+            smem, nitems, (unsigned long long)ncl);
+  ProfScope ps(s, "batch_band");
+  if (cudaLaunchKernelEx(&cfg, k_batch_band, g) != cudaSuccess ||
+      cudaGetLastError() != cudaSuccess)
+    return set_error("batch: cluster launch");
+  return false;
+}
+
+static bool launch_staged(cudaStream_t s, const BJob *d_jobs,
+                          const BItem *d_items, uint32_t nitems,
+                          uint32_t *counter, size_t smem, bool copyback) {
+  if (nitems == 0) return false;
+  const DeviceInfo &di = device_info();
+  auto kern = copyback ? k_batch_copyback : k_batch_gather;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return set_error("batch: smem attribute");
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kStageThreads,
+                                                    smem) != cudaSuccess ||
+      occ < 1)
+    return set_error("batch: occupancy");
+  const uint32_t grid =
+      (uint32_t)std::min<uint64_t>((uint64_t)di.sms * occ, nitems);
+  BatchArgs g;
+  g.jobs = d_jobs;
+  g.items = d_items;
+  g.nitems = nitems;
+  g.counter = counter;
+  g.status = nullptr;
+  ProfScope ps(s, copyback ? "batch_copyback" : "batch_gather");
+  kern<<<grid, kStageThreads, smem, s>>>(g);
+  if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
+  return false;
+}
+
+static bool launch_items(cudaStream_t s, const BJob *d_jobs,
+                         const BItem *d_items, uint32_t nitems,
+                         uint32_t *counter, size_t smem) {
+  if (nitems == 0) return false;
+  const DeviceInfo &di = device_info();
+  cudaError_t err = cudaFuncSetAttribute(
+      k_batch_bs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return set_error("batch: smem attribute");
+  int occ = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_bs,
+                                                      kBatchThreads, smem);
+  if (err != cudaSuccess || occ < 1) return set_error("batch: occupancy");
+  const uint32_t grid =
+      (uint32_t)std::min<uint64_t>((uint64_t)di.sms * occ, nitems);
+  BatchArgs g;
+  g.jobs = d_jobs;
+  g.items = d_items;
+  g.nitems = nitems;
+  g.counter = counter;
+  g.status = nullptr;
+  ProfScope ps(s, "batch_tiles");
+  k_batch_bs<<<grid, kBatchThreads, smem, s>>>(g);
+  if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
+  return false;
+}
+
+// Records the work of the planned batch on stream s.
+static size_t item_count(lm_batch_t bt) {
+  size_t n = bt->small.size() + bt->big.size();
+  for (int gi = 0; gi < kBandGroups; ++gi) n += bt->band[gi].size();
+  for (int w = 0; w < bt->nwaves; ++w)
+    n += bt->wgather[w].size() + bt->wcopy[w].size();
+  return n;
+}
+
+static size_t stage_bytes(lm_batch_t bt) {
+  return bt->jobs.size() * sizeof(BJob) + item_count(bt) * sizeof(BItem);
+}
+
+// Side streams and the events that fork them from, and join them back to,
+// the batch's stream (both work under stream capture).
+static bool ensure_side(lm_batch_t bt) {
+  if (bt->fork) return false;
+  if (cudaEventCreateWithFlags(&bt->fork, cudaEventDisableTiming) != cudaSuccess)
+    return set_error("batch: fork event");
+  for (int k = 0; k < kSideStreams; ++k) {
+    if (cudaStreamCreateWithFlags(&bt->side[k], cudaStreamNonBlocking) !=
+            cudaSuccess ||
+        cudaEventCreateWithFlags(&bt->join[k], cudaEventDisableTiming) !=
+            cudaSuccess)
+      return set_error("batch: side stream");
+  }
+  return false;
+}
+
+// Large jobs, longest first, each on the side stream with the least work so
+// far (greedy longest-processing-time order).
+static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
+                          unsigned flags) {
+  if (bt->large.empty()) return false;
+  std::vector<uint32_t> order(bt->large);
+  auto bytes_of = [&](uint32_t k) {
+    const Normalized &nz = bt->norm[k];
+    return nz.T * nz.a * nz.B * nz.b * (uint64_t)jobs[k].elem_bytes;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+    return bytes_of(x) > bytes_of(y);
+  });
+  const int nside = std::min<int>(kSideStreams, (int)order.size());
+  if (nside > 1 && ensure_side(bt)) return true;
+  if (nside > 1) {
+    cudaEventRecord(bt->fork, s);
+    for (int k = 0; k < nside; ++k) cudaStreamWaitEvent(bt->side[k], bt->fork, 0);
+  }
+  uint64_t load[kSideStreams] = {};
+  for (uint32_t k : order) {
+    int best = 0;
+    for (int q = 1; q < nside; ++q)
+      if (load[q] < load[best]) best = q;
+    load[best] += bytes_of(k);
+    const cudaStream_t qs = nside > 1 ? bt->side[best] : s;
+    const Normalized &nz = bt->norm[k];
+    if (run_0100_planned(qs, jobs[k].buf, jobs[k].elem_bytes, nz.T, nz.a,
+                         nz.B, nz.b, (flags & LM_BATCH_NO_TUNE) ? 0 : 1))
+      return true;
+  }
+  if (nside > 1) {
+    for (int k = 0; k < nside; ++k) {
+      cudaEventRecord(bt->join[k], bt->side[k]);
+      cudaStreamWaitEvent(s, bt->join[k], 0);
+    }
+  }
+  return false;
+}
+
+// Records the work of the planned batch on stream s; `stage` (pinned, at
+// least stage_bytes) holds the uploaded tables and must stay unchanged until
+// the upload has executed (for a captured graph: as long as the graph lives).
+static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
+                          unsigned flags, char *stage) {
+  const size_t nj = bt->jobs.size();
+  const size_t ni = item_count(bt);
+  if (grow(bt, std::max<size_t>(nj, 1), std::max<size_t>(ni, 1))) return true;
+  // the large jobs need no table: they start first, on the side streams
+  if (enqueue_large(bt, s, jobs, flags)) return true;
+  // stage: jobs, then small items, big items and the cluster groups.  The
+  // shared staging buffer is reused only after the previous upload from it
+  // has executed.
+  if (!stage && bt->uploaded) cudaEventSynchronize(bt->uploaded);
+  char *h = stage ? stage : (char *)bt->h_stage;
+  memcpy(h, bt->jobs.data(), nj * sizeof(BJob));
+  {
+    // staged jobs hold arena offsets until here
+    BJob *hj = reinterpret_cast<BJob *>(h);
+    for (size_t k = 0; k < nj; ++k)
+      if (hj[k].S) hj[k].scratch = bt->d_arena + (uintptr_t)hj[k].scratch;
+  }
+  {
+    BItem *dst = reinterpret_cast<BItem *>(h + nj * sizeof(BJob));
+    auto put = [&](const std::vector<BItem> &v) {
+      if (!v.empty()) memcpy(dst, v.data(), v.size() * sizeof(BItem));
+      dst += v.size();
+    };
+    put(bt->small);
+    put(bt->big);
+    for (int gi = 0; gi < kBandGroups; ++gi) put(bt->band[gi]);
+    for (int w = 0; w < bt->nwaves; ++w) {
+      put(bt->wgather[w]);
+      put(bt->wcopy[w]);
+    }
+  }
+  if (nj && cudaMemcpyAsync(bt->d_jobs, h, nj * sizeof(BJob),
+                            cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return set_error("batch: job upload");
+  if (ni && cudaMemcpyAsync(bt->d_items, h + nj * sizeof(BJob),
+                            ni * sizeof(BItem), cudaMemcpyHostToDevice,
+                            s) != cudaSuccess)
+    return set_error("batch: item upload");
+  if (!stage) {
+    if (!bt->uploaded &&
+        cudaEventCreateWithFlags(&bt->uploaded, cudaEventDisableTiming) !=
+            cudaSuccess)
+      return set_error("batch: upload event");
+    cudaEventRecord(bt->uploaded, s);
+  }
+  if (cudaMemsetAsync(bt->d_counters, 0, kCounterBytes, s) != cudaSuccess)
+    return set_error("batch: counter clear");
+  if (launch_items(s, bt->d_jobs, bt->d_items, (uint32_t)bt->small.size(),
+                   bt->d_counters, kSmallItem + 256))
+    return true;
+  size_t off = bt->small.size();
+  if (!bt->big.empty()) {
+    const DeviceInfo &di = device_info();
+    if (launch_items(s, bt->d_jobs, bt->d_items + off,
+                     (uint32_t)bt->big.size(), bt->d_counters + kCounterStride,
+                     (size_t)di.max_smem_optin - 1024))
+      return true;
+  }
+  off += bt->big.size();
+  for (int gi = 0; gi < kBandGroups; ++gi) {
+    if (launch_band(s, bt->d_jobs, bt->d_items + off,
+                    (uint32_t)bt->band[gi].size(),
+                    bt->d_counters + (2 + gi) * kCounterStride,
+                    bt->band_smem[gi], 2 << gi))
+      return true;
+    off += bt->band[gi].size();
+  }
+  for (int w = 0; w < bt->nwaves; ++w) {
+    uint32_t *c = bt->d_counters + (2 + kBandGroups + 2 * w) * kCounterStride;
+    if (launch_staged(s, bt->d_jobs, bt->d_items + off,
+                      (uint32_t)bt->wgather[w].size(), c, bt->wsmem[w], false))
+      return true;
+    off += bt->wgather[w].size();
+    if (launch_staged(s, bt->d_jobs, bt->d_items + off,
+                      (uint32_t)bt->wcopy[w].size(), c + kCounterStride, 0,
+                      true))
+      return true;
+    off += bt->wcopy[w].size();
+  }
+  return false;
+}
+
+extern "C" {
+
+bool lm_batch_create(lm_batch_t *out) {
+  if (!out) return set_error("batch: null handle pointer");
+  *out = new lm_batch_st();
+  cudaGetDevice(&(*out)->device);
+  device_status_word();  // allocate outside any capture
+  return false;
+}
+
+void lm_batch_destroy(lm_batch_t bt) {
+  if (!bt) return;
+  if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
+  if (bt->d_jobs) cudaFree(bt->d_jobs);
+  if (bt->d_items) cudaFree(bt->d_items);
+  if (bt->d_counters) cudaFree(bt->d_counters);
+  if (bt->d_arena) cudaFree(bt->d_arena);
+  if (bt->h_stage) cudaFreeHost(bt->h_stage);
+  if (bt->h_gstage) cudaFreeHost(bt->h_gstage);
+  if (bt->uploaded) cudaEventDestroy(bt->uploaded);
+  for (int k = 0; k < lm::kSideStreams; ++k) {
+    if (bt->side[k]) cudaStreamDestroy(bt->side[k]);
+    if (bt->join[k]) cudaEventDestroy(bt->join[k]);
+  }
+  if (bt->fork) cudaEventDestroy(bt->fork);
+  delete bt;
+}
+
+bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
+                  int njobs, unsigned flags) {
+  if (!bt) return set_error("batch: null handle");
+  if (njobs < 0 || (njobs > 0 && !jobs)) return set_error("batch: bad job list");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (flags & LM_BATCH_GRAPH) {
+    const uint64_t key = hash_jobs(jobs, njobs);
+    if (bt->gexec && key == bt->gkey) {
+      if (cudaGraphLaunch(bt->gexec, s) != cudaSuccess)
+        return set_error("batch: graph launch");
+      return false;
+    }
+    if (key == bt->seen_key) {
+      // second run of this job list: record it (everything it touches was
+      // initialised by the first run, outside any capture, and the tuned
+      // plans are cached), then replay
+      if (plan_batch(bt, jobs, njobs, flags)) return true;
+      if (grow(bt, std::max<size_t>(bt->jobs.size(), 1),
+               std::max<size_t>(item_count(bt), 1)))
+        return true;
+      if (bt->gexec) {
+        cudaGraphExecDestroy(bt->gexec);
+        bt->gexec = nullptr;
+      }
+      if (bt->h_gstage) cudaFreeHost(bt->h_gstage);
+      bt->h_gstage = nullptr;
+      if (cudaMallocHost(&bt->h_gstage, stage_bytes(bt) + 256) != cudaSuccess) {
+        bt->h_gstage = nullptr;
+        return set_error("batch: cannot allocate the graph's staging buffer");
+      }
+      cudaStream_t cs;
+      if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+        return set_error("batch: capture stream");
+      if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) !=
+          cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return set_error("batch: begin capture");
+      }
+      const bool failed = enqueue_batch(bt, cs, jobs, flags, (char *)bt->h_gstage);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+      cudaStreamDestroy(cs);
+      if (failed || ce != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        return failed ? true : set_error("batch: end capture");
+      }
+      if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
+      bt->gexec = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&bt->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) {
+        bt->gexec = nullptr;
+        return set_error("batch: graph instantiate");
+      }
+      bt->gkey = key;
+      if (cudaGraphLaunch(bt->gexec, s) != cudaSuccess)
+        return set_error("batch: graph launch");
+      return false;
+    }
+    bt->seen_key = key;
+  }
+  if (plan_batch(bt, jobs, njobs, flags)) return true;
+  return enqueue_batch(bt, s, jobs, flags, nullptr);
+}
+
+bool lm_batch_stats_get(lm_batch_t bt, lm_batch_stats *out) {
+  if (!bt || !out) return set_error("batch: null argument");
+  *out = bt->stats;
+  return false;
+}
+
+}  // extern "C"

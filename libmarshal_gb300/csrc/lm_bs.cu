@@ -14,10 +14,11 @@
 //    a few hundred CTAs, each streaming tens of KB;
 //  * tiles up to 227 KB fit one CTA (opt-in shared memory);
 //  * larger tiles are spread over a thread-block cluster of 2..16 CTAs: each
-//    CTA stages a band of rows, a cluster barrier separates load and store,
-//    and the store phase gathers its rows from the other CTAs' shared memory
-//    (distributed shared memory).  A 32 x 12289 fp32 tile (1.57 MB) fits an
-//    8-CTA cluster; the reference would fall back to PTTWAC;
+//    CTA stages a COLUMN band of every row and writes the output rows of that
+//    band (one contiguous range) from its own shared memory; the cluster
+//    barrier only orders all loads before all stores.  A 32 x 12289 fp32
+//    tile (1.57 MB) fits an 8-CTA cluster; the reference would fall back to
+//    PTTWAC;
 //  * rows are padded in shared memory so the transposed read (stride = one
 //    row) touches distinct banks; global loads and stores are coalesced;
 //  * the grid is persistent (at most the co-resident CTAs / clusters).
@@ -49,24 +50,15 @@ struct BsArgs {
 
 constexpr int kBsThreads = 512;
 constexpr int kBsUnroll = 8;
+constexpr uint32_t kBandMaxRows = 1024;  // rows of a tile in cluster form
 
-template <int E, bool CLUSTER>
+// One CTA per chunk of k consecutive tiles (k >= 1), staged whole.
+template <int E>
 __global__ void __launch_bounds__(kBsThreads) k_bs0100(BsArgs g) {
   using T = typename Elem<E>::T;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ unsigned char *rbase[16];
-  uint32_t C = 1, rank = 0;
-  uint64_t cid = blockIdx.x, ncl = gridDim.x;
-  if constexpr (CLUSTER) {
-    cg::cluster_group cl = cg::this_cluster();
-    C = cl.num_blocks();
-    rank = cl.block_rank();
-    cid = blockIdx.x / C;
-    ncl = gridDim.x / C;
-    if (threadIdx.x < C)
-      rbase[threadIdx.x] = cl.map_shared_rank(smem, (unsigned)threadIdx.x);
-    cl.sync();  // every CTA of the cluster is running before any DSMEM access
-  }
+  const uint32_t C = 1, rank = 0;
+  const uint64_t cid = blockIdx.x, ncl = gridDim.x;
 
   for (uint64_t chunk = cid; chunk < g.nchunks; chunk += ncl) {
     const uint64_t t0 = chunk * g.k;
@@ -100,10 +92,9 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100(BsArgs g) {
         }
       }
     }
-    if constexpr (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
+    __syncthreads();
 
-    // ---- store: my share of the chunk's outputs, gathered from the band
-    // owners' shared memory.
+    // ---- store: the chunk's outputs from the staged rows
     {
       const uint32_t nout = rows * g.row_elems;
       const uint32_t per = (nout + C - 1) / C;
@@ -128,14 +119,7 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100(BsArgs g) {
             const uint32_t i = u2 - j * g.a;
             const uint32_t row = t * g.a + i;
             const uint32_t col = j * g.b + sub;
-            const unsigned char *sb = smem;
-            uint32_t lrow = row;
-            if constexpr (CLUSTER) {
-              const uint32_t owner = fdiv(row, g.div_rpc);
-              lrow = row - owner * g.rpc;
-              sb = rbase[owner];
-            }
-            v[u] = *reinterpret_cast<const T *>(sb + lrow * g.pitch + col * E);
+            v[u] = *reinterpret_cast<const T *>(smem + row * g.pitch + col * E);
           }
         }
 #pragma unroll
@@ -145,8 +129,111 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100(BsArgs g) {
         }
       }
     }
-    // nobody reloads (or exits) while another CTA may still read its band
-    if constexpr (CLUSTER) cg::this_cluster().sync(); else __syncthreads();
+    __syncthreads();
+  }
+}
+
+// Cluster form for tiles larger than one CTA's shared memory: CTA r of the
+// cluster stages COLUMN band r (units [r*band, (r+1)*band) of every row of the
+// tile), so the output rows of its band -- one contiguous output range -- are
+// produced from its own shared memory.  The cluster barrier only separates
+// every CTA's loads from every CTA's stores (the output range of one band
+// overlaps input rows staged by the others); no shared memory is read across
+// CTAs.
+template <int E>
+__global__ void __launch_bounds__(kBsThreads) k_bs0100_band(BsArgs g) {
+  using T = typename Elem<E>::T;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t rowoff[kBandMaxRows];
+  __shared__ int s_ok;
+  cg::cluster_group cl = cg::this_cluster();
+  const uint32_t C = cl.num_blocks();
+  const uint32_t rank = cl.block_rank();
+  const uint64_t cid = blockIdx.x / C, ncl = gridDim.x / C;
+  const uint32_t bc0 = min(g.B, rank * g.rpc);  // rpc = units per band
+  const uint32_t bc1 = min(g.B, bc0 + g.rpc);
+  const uint32_t nbu = bc1 - bc0;               // units in my band
+  const uint32_t band_elems = nbu * g.b;
+  const uint32_t len = band_elems * E;          // bytes per row segment
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    s_ok = 1;
+  }
+  __syncthreads();
+  uint32_t parity = 0;
+  for (uint64_t tile = cid; tile < g.T; tile += ncl) {
+    const uint64_t e0 = tile * (uint64_t)g.tile_elems;
+    T *t = reinterpret_cast<T *>(g.base) + e0;
+    // ---- load: one bulk copy per row (16-byte aligned superset of the band
+    // segment; rowoff[] records where the segment starts in shared memory)
+    if (warp == 0 && len > 0) {
+      uint32_t bytes = 0;
+      for (uint32_t r = lane; r < g.a; r += 32) {
+        const char *src = reinterpret_cast<const char *>(
+            t + (uint64_t)r * g.row_elems + (uint64_t)bc0 * g.b);
+        const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+        const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+        bytes += (uint32_t)(a1 - a0);
+        rowoff[r] = r * g.pitch + (uint32_t)((uintptr_t)src - a0);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+      fence_proxy_async_smem();
+      if (lane == 0) mbar_arrive_expect_tx(&bar, bytes);
+      __syncwarp();
+      for (uint32_t r = lane; r < g.a; r += 32) {
+        const char *src = reinterpret_cast<const char *>(
+            t + (uint64_t)r * g.row_elems + (uint64_t)bc0 * g.b);
+        const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
+        const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
+        bulk_g2s(smem + (size_t)r * g.pitch, (const void *)a0,
+                 (uint32_t)(a1 - a0), &bar);
+      }
+    }
+    if (len > 0) {
+      const uint64_t t0 = global_timer_ns();
+      while (!mbar_try_wait(&bar, parity)) {
+        if (global_timer_ns() - t0 > 2000000000ull) {  // cannot happen: bounded anyway
+          s_ok = 0;
+          break;
+        }
+      }
+      parity ^= 1;
+    }
+    cl.sync();  // every band staged before any output is written
+    // ---- store: output rows bc0..bc1-1 = elements [bc0*a*b, bc1*a*b)
+    const uint32_t n = g.a * band_elems;
+    T *dst = t + (uint64_t)bc0 * g.a * g.b;
+    if (s_ok) {
+      for (uint32_t base = threadIdx.x; base < n;
+           base += kBsThreads * kBsUnroll) {
+        T v[kBsUnroll];
+#pragma unroll
+        for (int u = 0; u < kBsUnroll; ++u) {
+          const uint32_t o = base + u * kBsThreads;
+          if (o < n) {
+            uint32_t unit = o, sub = 0;
+            if (g.b != 1) {
+              unit = fdiv(o, g.div_b);
+              sub = o - unit * g.b;
+            }
+            const uint32_t j = fdiv(unit, g.div_a);  // output row in band
+            const uint32_t i = unit - j * g.a;
+            v[u] = *reinterpret_cast<const T *>(smem + rowoff[i] +
+                                                (j * g.b + sub) * E);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kBsUnroll; ++u) {
+          const uint32_t o = base + u * kBsThreads;
+          if (o < n) __stcg(dst + o, v[u]);
+        }
+      }
+    }
+    __syncthreads();  // my shared band is free for the next tile
   }
 }
 
@@ -168,8 +255,11 @@ BsPlan plan_bs0100(uint64_t T, uint32_t a, uint32_t B, uint32_t b, int e,
   const uint64_t tile_elems = row_elems * a;
   if (tile_elems >= 0xffffffffull) return p;
   const DeviceInfo &di = device_info();
+  // leave room for the kernels' static shared memory (the cluster form keeps
+  // a row-offset table of kBandMaxRows words)
   const size_t max_smem = (smem_budget ? smem_budget
-                                       : (size_t)di.max_smem_optin) - 256;
+                                       : (size_t)di.max_smem_optin) -
+                          (kBandMaxRows * 4 + 512);
   const uint64_t pitch = bs_pitch(row_elems * e, e);
   const uint64_t tile_smem = pitch * a;
   const uint64_t target = 40 * 1024;  // a few CTAs per SM overlap load/store
@@ -185,17 +275,27 @@ BsPlan plan_bs0100(uint64_t T, uint32_t a, uint32_t B, uint32_t b, int e,
     p.cluster = 1;
     p.rows_per_cta = a;
   } else {
+    // cluster of C CTAs, each staging a column band of ceil(B/C) units
     p.tiles_per_chunk = 1;
     for (int C = 2; C <= 16; C *= 2) {
-      const uint64_t rpc = (a + C - 1) / C;
-      if ((uint64_t)C > a) break;
-      if (rpc * pitch <= max_smem) {
+      if ((uint64_t)C > B) break;
+      const uint64_t band = (B + C - 1) / C;
+      // bulk-copy destination rows: 16-byte aligned, room for the aligned
+      // superset (up to 30 extra bytes), an odd number of 16-byte words
+      uint64_t bp = (band * b * e + 15) / 16 * 16 + 32;
+      if (((bp / 16) & 1) == 0) bp += 16;
+      if (a > kBandMaxRows) break;
+      if (bp * a <= max_smem) {
         p.cluster = C;
-        p.rows_per_cta = (uint32_t)rpc;
-        break;
+        p.rows_per_cta = (uint32_t)band;  // units per band in cluster form
+        p.pitch = (uint32_t)bp;
+        p.smem_bytes = (size_t)(bp * a);
+        p.threads = kBsThreads;
+        p.feasible = true;
+        return p;
       }
     }
-    if (p.rows_per_cta == 0) return p;
+    return p;
   }
   p.pitch = (uint32_t)pitch;
   p.smem_bytes = (size_t)p.rows_per_cta * pitch;
@@ -206,7 +306,7 @@ BsPlan plan_bs0100(uint64_t T, uint32_t a, uint32_t B, uint32_t b, int e,
 
 template <int E, bool CLUSTER>
 static cudaError_t run_bs(cudaStream_t s, const BsArgs &g, const BsPlan &p) {
-  auto kern = k_bs0100<E, CLUSTER>;
+  auto kern = CLUSTER ? k_bs0100_band<E> : k_bs0100<E>;
   const DeviceInfo &di = device_info();
   cudaError_t err = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
@@ -251,7 +351,7 @@ static cudaError_t run_bs(cudaStream_t s, const BsArgs &g, const BsPlan &p) {
   if (g.nchunks < ncl) ncl = g.nchunks;
   cfg.gridDim = dim3((unsigned)(ncl * p.cluster));
   if (getenv("LM_VERBOSE"))
-    fprintf(stderr, "bs_cluster: C=%d smem=%zu rpc=%u pitch=%u chunks=%llu "
+    fprintf(stderr, "bs_cluster: C=%d smem=%zu band=%u pitch=%u tiles=%llu "
             "max_clusters=%d grid=%u\n", p.cluster, p.smem_bytes,
             p.rows_per_cta, p.pitch, (unsigned long long)g.nchunks,
             max_clusters, cfg.gridDim.x);

@@ -98,6 +98,11 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
                             void *scratch, uint32_t *status,
                             uint64_t timeout_ns);
 
+// The per-op planner (lm_api.cu) for one 0100; tune != 0 lets the
+// autotuner pick the algorithm of this shape class.
+bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
+                      uint64_t a, uint64_t B, uint64_t b, int tune);
+
 // Per-device persistent status word that waiting kernels OR their failures
 // into (allocated on first use); lm_api.cu reads and clears it.
 uint32_t *device_status_word();

@@ -76,6 +76,9 @@ extern "C" bool lm_transpose_100_noalloc(lm_stream_t stream, void *buf,
     return set_error("lm_transpose_100_noalloc: dimensions must be >= 0");
   if (A <= 1 || B <= 1 || b == 0) return false;  // empty or identity
   if (buf == nullptr) return set_error("lm_transpose_100_noalloc: null buffer");
+  if (((uintptr_t)buf & (uintptr_t)(elem_bytes - 1)) != 0)
+    return set_error("lm_transpose_100_noalloc: buffer must be aligned to the "
+                     "element size");
   const size_t need = pttwac_flag_bytes(buf, 1, (uint32_t)A, (uint32_t)B,
                                         (uint32_t)b, elem_bytes);
   if (need == 0)

@@ -80,33 +80,44 @@ __host__ __device__ __forceinline__ uint64_t stash_rows(uint64_t J, uint64_t g,
   return r < A ? r : A;
 }
 
-// K0: stash offsets (one thread per group, then a single-block scan).
+// K0: stash offsets: per-thread partial sums over a range of groups, then a
+// block-wide exclusive scan of the 1024 partials (warp shuffles).
 __global__ void k_stash_offsets(uint64_t *soff, uint64_t A, uint64_t B,
                                 uint32_t g, uint32_t G, uint64_t row_bytes,
                                 uint64_t k) {
-  __shared__ uint64_t part[1024];
+  __shared__ uint64_t warp_tot[32];
   const uint32_t t = threadIdx.x, nt = blockDim.x;
+  const uint32_t lane = t & 31, warp = t >> 5;
   const uint32_t per = (G + nt - 1) / nt;
   const uint32_t j0 = min(G, t * per), j1 = min(G, j0 + per);
-  uint64_t s = 0;
-  for (uint32_t J = j0; J < j1; ++J) s += stash_rows(J, g, A, B, k) * row_bytes;
-  part[t] = s;
+  uint64_t part = 0;
+  for (uint32_t J = j0; J < j1; ++J) part += stash_rows(J, g, A, B, k) * row_bytes;
+  // inclusive scan within the warp
+  uint64_t inc = part;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t v = __shfl_up_sync(kFull, inc, o);
+    if (lane >= (uint32_t)o) inc += v;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
   __syncthreads();
-  if (t == 0) {
-    uint64_t acc = 0;
-    for (uint32_t i = 0; i < nt; ++i) {
-      const uint64_t v = part[i];
-      part[i] = acc;
-      acc += v;
+  if (warp == 0) {
+    const uint32_t nw = nt / 32;
+    uint64_t w = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t v = __shfl_up_sync(kFull, w, o);
+      if (lane >= (uint32_t)o) w += v;
     }
-    soff[G] = acc;
+    if (lane < nw) warp_tot[lane] = w;  // inclusive over warps
   }
   __syncthreads();
-  uint64_t acc = part[t];
+  uint64_t acc = inc - part + (warp ? warp_tot[warp - 1] : 0);
   for (uint32_t J = j0; J < j1; ++J) {
     soff[J] = acc;
     acc += stash_rows(J, g, A, B, k) * row_bytes;
   }
+  if (t == nt - 1) soff[G] = acc;
 }
 
 // K1: copy the rows that are overwritten before they are consumed.

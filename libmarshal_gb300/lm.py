@@ -52,6 +52,11 @@ _SIGS = {
     "lm_bs_feasible": (_I, [_LL, _I, _I, _I, _I]),
     "lm_debug_pad_stall": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _LL,
                                 ctypes.c_ulonglong]),
+    "lm_batch_create": (_B, [_VP]),
+    "lm_batch_destroy": (None, [_VP]),
+    "lm_batch_run": (_B, [_VP, _VP, _VP, _I, ctypes.c_uint]),
+    "lm_batch_stats_get": (_B, [_VP, _VP]),
+    "lm_tune_entries": (_I, []),
     "lm_launch_count": (ctypes.c_ulonglong, []),
     "lm_device_status": (ctypes.c_uint, [_VP]),
     "lm_prof_enable": (None, [_I]),
@@ -246,6 +251,73 @@ def prof_collect():
     n = lib().lm_prof_collect(ctypes.cast(arr, ctypes.c_void_p), cap)
     return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms))
             for i in range(min(n, cap))}
+
+
+# ---- batched conversion ------------------------------------------------------
+
+OP_0100, OP_010, OP_100, OP_AOS_ASTA, OP_ASTA_AOS, OP_SOA_ASTA, OP_ASTA_SOA, \
+    OP_TRANSPOSE = range(8)
+BATCH_GRAPH, BATCH_NO_TUNE, BATCH_NO_CLUSTER, BATCH_NO_SCRATCH = 1, 2, 4, 8
+
+
+class Job(ctypes.Structure):
+    """lm_job of include/lm_marshal.h."""
+    _fields_ = [("buf", ctypes.c_void_p), ("elem_bytes", ctypes.c_int),
+                ("op", ctypes.c_int), ("d0", ctypes.c_longlong),
+                ("d1", ctypes.c_longlong), ("d2", ctypes.c_longlong),
+                ("d3", ctypes.c_longlong)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_ulonglong) for n in (
+        "bytes", "small_bytes", "big_bytes", "large_bytes", "small_jobs",
+        "big_jobs", "large_jobs", "identity", "small_items", "big_items",
+        "band_bytes", "band_jobs", "band_items", "staged_bytes",
+        "staged_jobs", "staged_waves")]
+
+
+class Batch:
+    """Owner of an lm_batch_t: run(jobs) converts every job in place."""
+
+    def __init__(self):
+        self.h = ctypes.c_void_p()
+        _check(lib().lm_batch_create(ctypes.byref(self.h)), "lm_batch_create")
+
+    def run(self, jobs, stream=None, graph=False, tune=True, cluster=True,
+            scratch=True):
+        arr = (Job * len(jobs))()
+        for i, j in enumerate(jobs):
+            arr[i] = j
+        flags = ((BATCH_GRAPH if graph else 0) | (0 if tune else BATCH_NO_TUNE)
+                 | (0 if cluster else BATCH_NO_CLUSTER)
+                 | (0 if scratch else BATCH_NO_SCRATCH))
+        _check(lib().lm_batch_run(self.h, stream_ptr(stream),
+                                  ctypes.cast(arr, ctypes.c_void_p),
+                                  len(jobs), flags), "lm_batch_run")
+
+    def stats(self):
+        st = BatchStats()
+        _check(lib().lm_batch_stats_get(self.h, ctypes.byref(st)),
+               "lm_batch_stats_get")
+        return {n: getattr(st, n) for n, _ in BatchStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().lm_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def job(buf, op, dims, elem_bytes=None):
+    """lm_job for a CUDA tensor (or raw pointer) and up to four dims."""
+    p, e = buf_ptr(buf, elem_bytes)
+    d = list(dims) + [0] * (4 - len(dims))
+    return Job(p, e, op, *d)
 
 
 def finalize() -> None:

@@ -1,0 +1,194 @@
+"""Batched conversion (lm_batch_*): every job of a mixed batch, bit-exact
+against the oracle, with and without CUDA-graph replay."""
+import numpy as np
+import pytest
+
+from oracle import lm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_of(op, src, d):
+    from libmarshal_gb300 import lm
+    if op == lm.OP_0100:
+        return O.t0100(src, *d[:4])
+    if op == lm.OP_010:
+        return O.t010(src, *d[:3])
+    if op == lm.OP_100:
+        return O.t100(src, *d[:3])
+    if op == lm.OP_AOS_ASTA:
+        return O.aos_asta(src, *d[:3])
+    if op == lm.OP_ASTA_AOS:
+        h, w, t = d[:3]
+        return O.t010(src, h // t, w, t)
+    if op == lm.OP_SOA_ASTA:
+        return O.soa_asta(src, *d[:3])
+    if op == lm.OP_ASTA_SOA:
+        h, w, t = d[:3]
+        return O.t100(src, h // t, w, t)
+    if op == lm.OP_TRANSPOSE:
+        return O.transpose(src, *d[:2])
+    raise ValueError(op)
+
+
+def make_jobs(seed, n, lo, hi, big=()):
+    from libmarshal_gb300 import lm
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n):
+        e = int(rng.choice([1, 2, 4, 8]))
+        h = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        w = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        kind = int(rng.integers(0, 8))
+        t = int(rng.choice([16, 32, 64]))
+        if kind == 0:
+            op, d = lm.OP_TRANSPOSE, (h, w)
+        elif kind == 1:
+            op, d = lm.OP_AOS_ASTA, ((h + t - 1) // t * t, w, t)
+        elif kind == 2:
+            op, d = lm.OP_ASTA_AOS, ((h + t - 1) // t * t, w, t)
+        elif kind == 3:
+            op, d = lm.OP_SOA_ASTA, ((h + t - 1) // t * t, w, t)
+        elif kind == 4:
+            op, d = lm.OP_ASTA_SOA, ((h + t - 1) // t * t, w, t)
+        elif kind == 5:
+            op, d = lm.OP_100, (h, w, int(rng.choice([1, 2, 3])))
+        elif kind == 6:
+            op, d = lm.OP_010, (max(1, h // 16), 16, w)
+        else:
+            op, d = lm.OP_0100, (2, max(1, h // 8), w // 4 + 1, 3)
+        specs.append((op, d, e))
+    specs += list(big)
+    return specs
+
+
+def nelems(op, d):
+    from libmarshal_gb300 import lm
+    if op == lm.OP_0100:
+        return d[0] * d[1] * d[2] * d[3]
+    if op in (lm.OP_010, lm.OP_100):
+        return d[0] * d[1] * d[2]
+    if op == lm.OP_TRANSPOSE:
+        return d[0] * d[1]
+    return d[0] * d[1]
+
+
+def run_and_check(cuda, specs, graph, reps, **flags):
+    import torch
+    from libmarshal_gb300 import lm
+    srcs, bufs, jobs = [], [], []
+    for k, (op, d, e) in enumerate(specs):
+        n = nelems(op, d)
+        src = O.random_bits(n, e, 1000 + k)
+        srcs.append(src)
+        b = torch.from_numpy(src.view(np.uint8).copy()).to(cuda)
+        bufs.append(b)
+        jobs.append(lm.job(b, op, d, elem_bytes=e))
+    want = [oracle_of(op, s, d) for (op, d, e), s in zip(specs, srcs)]
+    bt = lm.Batch()
+    for rep in range(reps):
+        if rep:
+            for b, s in zip(bufs, srcs):  # same buffers, original data
+                b.copy_(torch.from_numpy(s.view(np.uint8).copy()).to(cuda))
+        bt.run(jobs, graph=graph, **flags)
+        torch.cuda.synchronize()
+        for k, ((op, d, e), b) in enumerate(zip(specs, bufs)):
+            got = b.cpu().numpy().view(O.DTYPES[e])
+            assert np.array_equal(got, want[k]), (rep, k, op, d, e)
+    st = bt.stats()
+    bt.close()
+    assert lm.lib().lm_device_status(None) == 0
+    return st
+
+
+def test_batch_small_mixed(cuda):
+    from libmarshal_gb300 import lm
+    specs = make_jobs(1, 300, 16, 300)
+    st = run_and_check(cuda, specs, graph=False, reps=1)
+    assert st["small_jobs"] > 0
+
+
+BIG = [(7, (2048, 1031), 4), (3, (4096, 3000, 64), 8), (7, (1500, 1700), 2),
+       (2, (4096, 1000, 1), 1), (5, (1 << 16, 4, 32), 4),
+       (0, (3, 1100, 700, 3), 2), (2, (2000, 1500, 2), 8)]
+
+
+def test_batch_with_large_jobs_and_graph(cuda):
+    specs = make_jobs(2, 120, 16, 1200, big=BIG)
+    st = run_and_check(cuda, specs, graph=True, reps=3)
+    assert st["staged_jobs"] > 0 and (st["small_jobs"] + st["big_jobs"]) > 0
+
+
+def test_batch_strictly_in_place(cuda):
+    """LM_BATCH_NO_SCRATCH: large jobs go through the in-place planner."""
+    specs = make_jobs(4, 60, 16, 1200, big=BIG)
+    st = run_and_check(cuda, specs, graph=True, reps=3, scratch=False)
+    assert st["staged_jobs"] == 0 and st["large_jobs"] > 0
+
+
+def test_batch_staged_waves(cuda, monkeypatch):
+    """A small arena: several waves, jobs above it fall back to the planner."""
+    monkeypatch.setenv("LM_BATCH_SCRATCH_MB", "9")
+    specs = make_jobs(5, 60, 16, 1200, big=BIG + [(7, (777, 2999), 1)] * 3)
+    st = run_and_check(cuda, specs, graph=True, reps=3)
+    assert st["staged_waves"] > 1 and st["large_jobs"] > 0
+
+
+def test_batch_rejects_bad_jobs(cuda):
+    import torch
+    from libmarshal_gb300 import lm
+    b = torch.zeros(64, dtype=torch.uint8, device=cuda)
+    bt = lm.Batch()
+    with pytest.raises(lm.LMError):
+        bt.run([lm.job(b, lm.OP_AOS_ASTA, (10, 3, 4), elem_bytes=1)])
+    with pytest.raises(lm.LMError):
+        bt.run([lm.job(b, lm.OP_TRANSPOSE, (8, 8), elem_bytes=3)])
+    bt.run([lm.job(b, lm.OP_TRANSPOSE, (1, 64), elem_bytes=1)])  # identity
+    bt.close()
+
+
+# Tiles too large for one CTA's shared memory but small enough for a cluster
+# of 2..16 CTAs (column bands of at most ~222 KB each), with odd, unaligned
+# row lengths and every element width.
+BAND_SPECS = [
+    (7, (256, 300), 4),                 # clusters of 4
+    (7, (333, 777), 2),                 # unaligned rows, clusters of 8
+    (3, (64 * 7, 3000, 64), 8),         # 7 tiles of 64 x 3000
+    (2, (500, 999, 3), 1),              # b = 3, bytes
+    (7, (600, 700), 4),                 # one CTA per SM per band
+    (7, (1000, 800), 4),                # clusters of 16
+    (0, (5, 100, 2000, 1), 4),          # 5 tiles
+    (0, (3, 200, 300, 5), 8),           # b = 5, 8-byte elements
+    (4, (64 * 5, 1000, 64), 8),         # ASTA -> AoS, 1000-row tiles
+]
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_cluster_items(cuda, graph):
+    specs = make_jobs(3, 40, 16, 200, big=BAND_SPECS)
+    st = run_and_check(cuda, specs, graph=graph, reps=3 if graph else 1)
+    assert st["band_jobs"] == len(BAND_SPECS), st
+    assert st["band_items"] >= st["band_jobs"]
+
+
+def test_batch_cluster_off_matches(cuda):
+    """LM_BATCH_NO_CLUSTER sends the same jobs through the per-op planner."""
+    import torch
+    from libmarshal_gb300 import lm
+    srcs, outs = [], []
+    for cluster in (True, False):
+        bufs, jobs = [], []
+        for k, (op, d, e) in enumerate(BAND_SPECS):
+            src = O.random_bits(nelems(op, d), e, 77 + k)
+            b = torch.from_numpy(src.view(np.uint8).copy()).to(cuda)
+            bufs.append(b)
+            jobs.append(lm.job(b, op, d, elem_bytes=e))
+        bt = lm.Batch()
+        bt.run(jobs, cluster=cluster)
+        torch.cuda.synchronize()
+        st = bt.stats()
+        bt.close()
+        assert (st["band_jobs"] > 0) == cluster
+        outs.append([b.cpu().numpy() for b in bufs])
+    for x, y in zip(*outs):
+        assert np.array_equal(x, y)

@@ -52,6 +52,13 @@ def test_library_reports_errors_without_a_gpu_call(built):
     assert "multiple" in lm.last_error()
     assert L.lm_transpose_100(None, None, 3, 4, 5, 1, None) is True
     assert "element size" in lm.last_error()
+    # a 4-byte element at an odd address is refused before any launch
+    assert L.lm_transpose_100(None, 0x1002, 4, 4, 5, 1, None) is True
+    assert "aligned" in lm.last_error()
+    assert L.lm_transpose_100_noalloc(None, 0x1004, 8, 4, 5, 1) is True
+    assert "aligned" in lm.last_error()
+    assert L.lm_padding(None, 0x1001, 2, 3, 4, 5, None) is True
+    assert "aligned" in lm.last_error()
 
 
 def _fastdiv(d):
