@@ -403,7 +403,7 @@ def run_batch_workload(args, ws, rank, local):
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     L = lm.lib()
-    specs = batch_specs()
+    specs = batch_specs(n=args.batch_n)
     sizes = [d[0] * d[1] * e for (_, d, e) in specs]
     offs, tot = [], 0
     for nb in sizes:
@@ -445,7 +445,8 @@ def run_batch_workload(args, ws, rank, local):
 
     k = max(3, min(args.steps, 10))
     w = max(3, args.warmup)
-    ms_plain, l_plain = timed(plain_step, k, w)
+    ms_plain, l_plain = (float("nan"), 0) if args.skip_plain else \
+        timed(plain_step, k, w)
     ms_batch, l_batch = timed(lambda: bt.run(jobs, stream=stream), k, w)
     ms_graph, _ = timed(lambda: bt.run(jobs, stream=stream, graph=True), k, w)
     lm.prof_collect()
@@ -496,6 +497,10 @@ def main():
                     help="skip the CPU-baseline leg")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "batch", "serve"])
+    ap.add_argument("--batch-n", type=int, default=4096,
+                    help="matrices in the batched workload")
+    ap.add_argument("--skip-plain", action="store_true",
+                    help="batched workload: skip the per-request loop")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -38,7 +38,7 @@ constexpr int kCounterStride = 32;   // counters 128 bytes apart
 constexpr size_t kCounterBytes =
     (size_t)(2 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
 constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
-constexpr int kSideStreams = 4;      // streams the large jobs spread over
+constexpr int kSideStreams = 5;      // streams of the large jobs and groups
 
 struct BJob {
   char *base;
@@ -53,6 +53,10 @@ struct BJob {
   uint32_t S, nJ, nIJ;
   FastDiv div_Sb, div_nJ, div_nIJ;
   uint64_t bytes;
+  // b == 1 stores: groups of 8 staged rows (ceil(a/8) for bands, S/8 for
+  // staged blocks)
+  uint32_t ng8;
+  FastDiv div_ng8;
 };
 
 struct BItem {
@@ -67,6 +71,7 @@ struct BatchArgs {
   uint32_t nitems;
   uint32_t *counter;
   uint32_t *status;  // set to kStatusWaitTimeout if a staged load never lands
+  uint32_t stage_bytes;  // staged gather: bytes of one shared-memory stage
 };
 
 template <int E>
@@ -144,123 +149,242 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_bs(BatchArgs g) {
   }
 }
 
+// Warp 0: copies a job descriptor into shared memory (read there by every
+// thread instead of being held in registers).
+__device__ __forceinline__ void copy_job(BJob *dst, const BJob *src) {
+  static_assert(sizeof(BJob) % 4 == 0, "BJob is copied in 32-bit words");
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t k = lane; k < sizeof(BJob) / 4; k += 32)
+    reinterpret_cast<uint32_t *>(dst)[k] =
+        reinterpret_cast<const uint32_t *>(src)[k];
+}
+
+// Writes nrows x ncols staged elements (b == 1) transposed: output row jj
+// (stride `ostride` elements from `dst`) gets staged column jj.  A warp
+// reads an 8-row x 4-column patch per step, so its 32 lanes hit rows that
+// start in distinct 16-byte bank groups, and writes 4 output segments of 8
+// elements; work units are 8 rows x 16 columns, spread over all warps.
+template <int E>
+__device__ __forceinline__ void store_b1(const unsigned char *buf,
+                                         const uint32_t *rowoff, uint32_t nrows,
+                                         uint32_t ncols, uint32_t ng8,
+                                         const FastDiv &div_ng8,
+                                         typename Elem<E>::T *dst,
+                                         uint32_t ostride, uint32_t warp,
+                                         uint32_t nwarps) {
+  using T = typename Elem<E>::T;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t r = lane & 7, c = lane >> 3;
+  const uint32_t nch = (ncols + 15) / 16;
+  const uint32_t nunits = ng8 * nch;
+  for (uint32_t u0 = warp; u0 < nunits; u0 += nwarps) {
+    const uint32_t ch = fdiv(u0, div_ng8);
+    const uint32_t i = (u0 - ch * ng8) * 8 + r;
+    if (i >= nrows) continue;
+    const unsigned char *row = buf + rowoff[i];
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t jj = ch * 16 + u * 4 + c;
+      if (jj < ncols) v[u] = *reinterpret_cast<const T *>(row + jj * E);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t jj = ch * 16 + u * 4 + c;
+      if (jj < ncols) __stcg(dst + (uint64_t)jj * ostride + i, v[u]);
+    }
+  }
+}
+
 // Tiles larger than one CTA's shared memory, processed by persistent
-// clusters: rank 0 claims the next item and shares it through distributed
-// shared memory; each CTA stages a column band of the tile with bulk copies
+// clusters: rank 0 claims items and shares them through distributed shared
+// memory; each CTA stages a column band of the tile with bulk copies
 // (16-byte aligned supersets of the row segments) and writes the output rows
-// of its band from its own shared memory.
+// of its band from its own shared memory.  Two stages: the band of the next
+// item loads while the current one is written.
 constexpr uint32_t kBandMaxRows = 1024;
 namespace cgb = cooperative_groups;
 
-template <int E>
-__device__ void band_item(const BJob &j, uint64_t tile, uint32_t rank,
-                          unsigned char *smem, uint32_t *rowoff,
-                          uint64_t *bar, uint32_t &parity, int *s_ok,
-                          uint32_t *status, cgb::cluster_group &cl) {
-  using T = typename Elem<E>::T;
-  const uint32_t bc0 = min(j.B, rank * j.band);
-  const uint32_t bc1 = min(j.B, bc0 + j.band);
-  const uint32_t band_elems = (bc1 - bc0) * j.b;
-  // after a load that never landed this CTA stages nothing more (its shared
-  // memory may still be written) but keeps joining the cluster barriers
-  const uint32_t len = *s_ok ? band_elems * E : 0;
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T *t = reinterpret_cast<T *>(j.base) + tile * (uint64_t)j.tile_elems;
-  if (warp == 0 && len > 0) {
-    uint32_t bytes = 0;
-    for (uint32_t r = lane; r < j.a; r += 32) {
-      const char *src = reinterpret_cast<const char *>(
-          t + (uint64_t)r * j.row_elems + (uint64_t)bc0 * j.b);
-      const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
-      const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
-      bytes += (uint32_t)(a1 - a0);
-      rowoff[r] = r * j.pitch + (uint32_t)((uintptr_t)src - a0);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
-    fence_proxy_async_smem();
-    if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
-    __syncwarp();
-    for (uint32_t r = lane; r < j.a; r += 32) {
-      const char *src = reinterpret_cast<const char *>(
-          t + (uint64_t)r * j.row_elems + (uint64_t)bc0 * j.b);
-      const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
-      const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
-      bulk_g2s(smem + (size_t)r * j.pitch, (const void *)a0,
-               (uint32_t)(a1 - a0), bar);
-    }
-  }
-  if (len > 0) {
-    const uint64_t t0 = global_timer_ns();
-    while (!mbar_try_wait(bar, parity))
-      if (global_timer_ns() - t0 > 2000000000ull) {
-        *s_ok = 0;  // every thread of the CTA times out alike
-        if (threadIdx.x == 0) atomicExch(status, kStatusWaitTimeout);
-        break;
-      }
-    parity ^= 1;
-  }
-  cl.sync();  // every band of this tile staged before any output is written
-  const uint32_t n = j.a * band_elems;
-  T *dst = t + (uint64_t)bc0 * j.a * j.b;
-  if (len > 0 && *s_ok) {
-    for (uint32_t base = threadIdx.x; base < n; base += kBatchThreads * 4) {
-      T v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const uint32_t o = base + u * kBatchThreads;
-        if (o < n) {
-          uint32_t unit = o, sub = 0;
-          if (j.b != 1) {
-            unit = fdiv(o, j.div_b);
-            sub = o - unit * j.b;
-          }
-          const uint32_t jj = fdiv(unit, j.div_a);
-          const uint32_t i = unit - jj * j.a;
-          v[u] = *reinterpret_cast<const T *>(smem + rowoff[i] +
-                                              (jj * j.b + sub) * E);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const uint32_t o = base + u * kBatchThreads;
-        if (o < n) __stcg(dst + o, v[u]);
-      }
-    }
-  }
-  __syncthreads();
+struct BandPos {
+  uint32_t bc0, len;  // first unit of my band, bytes of my row segments
+};
+
+__device__ __forceinline__ BandPos band_pos(const BJob &j, uint32_t rank) {
+  BandPos p;
+  p.bc0 = min(j.B, rank * j.band);
+  const uint32_t bc1 = min(j.B, p.bc0 + j.band);
+  p.len = (bc1 - p.bc0) * j.b * j.e;
+  return p;
 }
 
-__global__ void __launch_bounds__(kBatchThreads) k_batch_band(BatchArgs g) {
+// Warp 0: bulk copies of my band of every row of `tile`.
+__device__ void band_issue(const BJob &j, uint64_t tile, uint32_t rank,
+                           unsigned char *buf, uint32_t *rowoff, uint64_t *bar) {
+  const uint32_t lane = threadIdx.x & 31;
+  const BandPos p = band_pos(j, rank);
+  if (p.len == 0) return;
+  const uint64_t row_bytes = (uint64_t)j.row_elems * j.e;
+  const char *row0 =
+      j.base + (tile * j.tile_elems + (uint64_t)p.bc0 * j.b) * j.e;
+  uint32_t bytes = 0;
+  for (uint32_t r = lane; r < j.a; r += 32) {
+    const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
+    const uintptr_t a0 = src & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + p.len + 15) & ~(uintptr_t)15;
+    bytes += (uint32_t)(a1 - a0);
+    rowoff[r] = r * j.pitch + (uint32_t)(src - a0);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+  fence_proxy_async_smem();
+  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+  __syncwarp();
+  for (uint32_t r = lane; r < j.a; r += 32) {
+    const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
+    const uintptr_t a0 = src & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + p.len + 15) & ~(uintptr_t)15;
+    bulk_g2s(buf + (size_t)r * j.pitch, (const void *)a0, (uint32_t)(a1 - a0),
+             bar);
+  }
+}
+
+// All threads: output rows of my band (one contiguous range of the tile).
+template <int E>
+__device__ void band_store(const BJob &j, uint64_t tile, uint32_t rank,
+                           const unsigned char *buf, const uint32_t *rowoff,
+                           uint32_t t, uint32_t nt) {
+  using T = typename Elem<E>::T;
+  const BandPos p = band_pos(j, rank);
+  const uint32_t n = j.a * (p.len / E);
+  T *dst = reinterpret_cast<T *>(j.base) + tile * (uint64_t)j.tile_elems +
+           (uint64_t)p.bc0 * j.a * j.b;
+  if (j.b == 1) {
+    store_b1<E>(buf, rowoff, j.a, p.len / E, j.ng8, j.div_ng8, dst, j.a,
+                t >> 5, nt >> 5);
+    return;
+  }
+  for (uint32_t base = t; base < n; base += nt * 4) {
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t o = base + u * nt;
+      if (o < n) {
+        const uint32_t unit = fdiv(o, j.div_b);
+        const uint32_t sub = o - unit * j.b;
+        const uint32_t jj = fdiv(unit, j.div_a);
+        const uint32_t i = unit - jj * j.a;
+        v[u] = *reinterpret_cast<const T *>(buf + rowoff[i] +
+                                            (jj * j.b + sub) * E);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t o = base + u * nt;
+      if (o < n) __stcg(dst + o, v[u]);
+    }
+  }
+}
+
+// Warp 0 is the producer: it waits for the bulk copies of item n, arrives
+// on the cluster barrier with release semantics (its shared-memory writes:
+// job, row offsets, rank 0's claims), then issues the copies of item n+1.
+// The other warps write item n and arrive relaxed: the barrier only has to
+// order every CTA's completed loads of a tile before any CTA's stores to it,
+// and a relaxed arrive does not wait for the earlier global stores to drain.
+__global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ uint32_t rowoff[kBandMaxRows];
-  __shared__ uint32_t s_item;
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t rowoff[2][kBandMaxRows];
+  __shared__ uint32_t s_item[2];  // rank 0's claims, by sequence parity
   __shared__ int s_ok;
+  __shared__ __align__(16) BJob s_jobs[2];   // job of the item in each stage
+  __shared__ uint64_t s_tile[2];
   cgb::cluster_group cl = cgb::this_cluster();
   const uint32_t rank = cl.block_rank();
+  const uint32_t warp = threadIdx.x >> 5;
+  const bool leader = rank == 0 && threadIdx.x == 0;
   if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     fence_mbar_init();
     s_ok = 1;
   }
-  uint32_t *item0 = cl.map_shared_rank(&s_item, 0);
-  uint32_t parity = 0;
-  while (true) {
-    if (rank == 0 && threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
-    cl.sync();  // rank 0's claim is visible; also orders the mbarrier init
-    const uint32_t k = *item0;
-    if (k >= g.nitems) break;
-    const BItem it = g.items[k];
-    const BJob j = g.jobs[it.job];
-    switch (j.e) {
-      case 1: band_item<1>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
-      case 2: band_item<2>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
-      case 4: band_item<4>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
-      default: band_item<8>(j, it.tile0, rank, smem, rowoff, &bar, parity, &s_ok, g.status, cl); break;
+  if (leader) s_item[0] = atomicAdd(g.counter, 1u);
+  cl.sync();  // claim 0 visible; barriers initialised
+  const uint32_t *item0 = cl.map_shared_rank(&s_item[0], 0);
+  uint32_t cur = item0[0];
+  if (leader) s_item[1] = atomicAdd(g.counter, 1u);  // read after the next sync
+  uint32_t parity = 0, pending = 0;
+  if (cur < g.nitems && warp == 0) {
+    const BItem it = g.items[cur];
+    copy_job(&s_jobs[0], &g.jobs[it.job]);
+    if ((threadIdx.x & 31) == 0) s_tile[0] = it.tile0;
+    band_issue(g.jobs[it.job], it.tile0, rank, smem, rowoff[0], &bar[0]);
+  }
+  for (uint32_t n = 0; cur < g.nitems; ++n) {
+    const int st = n & 1, nx = st ^ 1;
+    if (warp == 0) {
+      const BandPos p = band_pos(s_jobs[st], rank);
+      if (p.len > 0 && s_ok) {
+        bool landed = true;
+        const uint64_t t0 = global_timer_ns();
+        while (!mbar_try_wait(&bar[st], (parity >> st) & 1))
+          if (global_timer_ns() - t0 > 2000000000ull) {
+            landed = false;
+            break;
+          }
+        if (__all_sync(kFull, landed)) {
+          parity ^= 1u << st;
+        } else {
+          pending |= 1u << st;
+          if ((threadIdx.x & 31) == 0) {
+            s_ok = 0;  // stage nothing more, write nothing more
+            atomicExch(g.status, kStatusWaitTimeout);
+          }
+        }
+      }
+      cluster_arrive_release();
+    } else {
+      cluster_arrive_relaxed();
+    }
+    cluster_wait_acquire();  // every band of item n staged; claim n+1 visible
+    const uint32_t nxt = item0[nx];
+    if (warp == 0) {
+      if (nxt < g.nitems) {
+        const BItem in = g.items[nxt];
+        copy_job(&s_jobs[nx], &g.jobs[in.job]);
+        if ((threadIdx.x & 31) == 0) s_tile[nx] = in.tile0;
+        __syncwarp();
+        if (s_ok)
+          band_issue(g.jobs[in.job], in.tile0, rank,
+                     smem + (size_t)nx * g.stage_bytes, rowoff[nx], &bar[nx]);
+      }
+      if (leader) s_item[st] = atomicAdd(g.counter, 1u);  // claim n+2
+    } else if (s_ok) {
+      const BJob &j = s_jobs[st];
+      const unsigned char *buf = smem + (size_t)st * g.stage_bytes;
+      const uint64_t tile = s_tile[st];
+      const uint32_t t = threadIdx.x - 32, nt = kBatchThreads - 32;
+      switch (j.e) {
+        case 1: band_store<1>(j, tile, rank, buf, rowoff[st], t, nt); break;
+        case 2: band_store<2>(j, tile, rank, buf, rowoff[st], t, nt); break;
+        case 4: band_store<4>(j, tile, rank, buf, rowoff[st], t, nt); break;
+        default: band_store<8>(j, tile, rank, buf, rowoff[st], t, nt); break;
+      }
+    }
+    cur = nxt;
+  }
+  // a stage whose loads never landed: give them one more bounded wait
+  if (warp == 0) {
+    for (int st = 0; st < 2; ++st) {
+      if (!((pending >> st) & 1)) continue;
+      const uint64_t t0 = global_timer_ns();
+      while (!mbar_try_wait(&bar[st], (parity >> st) & 1) &&
+             global_timer_ns() - t0 < 2000000000ull) {
+      }
     }
   }
-  cl.sync();  // nobody leaves while rank 0's s_item may still be read
+  cl.sync();  // rank 0's claims stay readable until every CTA is done
 }
 
 // Staged form, for tiles too large for any on-chip plan: each S x S block of
@@ -270,90 +394,199 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_band(BatchArgs g) {
 // blocks (gather) or of 16-byte vectors (copy back).
 constexpr int kStageThreads = 256;
 constexpr uint32_t kStageTileBytes = 32 * 1024;  // S*S*b*e at most
+constexpr uint32_t kStageMaxS = 128;
 constexpr uint32_t kStageBlocksPerItem = 16;
 constexpr uint64_t kCopyVecsPerItem = 16384;     // 256 KB
 
-template <int E>
-__device__ void gather_block(const BJob &j, uint32_t q, unsigned char *smem) {
-  using T = typename Elem<E>::T;
-  const uint32_t t = fdiv(q, j.div_nIJ);
-  const uint32_t r = q - t * j.nIJ;
+// Block q of a staged job: tile t, block row bi, block column bj.
+struct GBlock {
+  uint32_t t, i0, j0, si, sj;
+};
+
+__device__ __forceinline__ GBlock gather_decode(const BJob &j, uint32_t q) {
+  GBlock k;
+  k.t = fdiv(q, j.div_nIJ);
+  const uint32_t r = q - k.t * j.nIJ;
   const uint32_t bi = fdiv(r, j.div_nJ);
   const uint32_t bj = r - bi * j.nJ;
-  const uint32_t i0 = bi * j.S, j0 = bj * j.S;
-  const uint32_t si = min(j.S, j.a - i0), sj = min(j.S, j.B - j0);
-  const uint32_t Sb = j.S * j.b;
-  const uint32_t n = j.S * Sb;  // a full block; edge blocks skip the rest
-  const T *src = reinterpret_cast<const T *>(j.base) +
-                 (uint64_t)t * j.tile_elems + (uint64_t)i0 * j.row_elems +
-                 (uint64_t)j0 * j.b;
-  T *dst = reinterpret_cast<T *>(j.scratch) + (uint64_t)t * j.tile_elems +
-           ((uint64_t)j0 * j.a + i0) * j.b;
-  const uint32_t lim_c = sj * j.b, lim_o = si * j.b;
-  for (uint32_t base = threadIdx.x; base < n; base += kStageThreads * 4) {
-    T v[4];
-    uint32_t sm[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t idx = base + u * kStageThreads;
-      const uint32_t rr = fdiv(idx, j.div_Sb);
-      const uint32_t c = idx - rr * Sb;
-      sm[u] = 0xffffffffu;
-      if (idx < n && rr < si && c < lim_c) {
-        v[u] = __ldcs(src + (uint64_t)rr * j.row_elems + c);
-        sm[u] = rr * j.pitch + c * E;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (sm[u] != 0xffffffffu) *reinterpret_cast<T *>(smem + sm[u]) = v[u];
+  k.i0 = bi * j.S;
+  k.j0 = bj * j.S;
+  k.si = min(j.S, j.a - k.i0);
+  k.sj = min(j.S, j.B - k.j0);
+  return k;
+}
+
+// Warp 0: one bulk copy per row of the block (the 16-byte aligned superset
+// of its row segment) into `buf`; rowoff[] records where each segment starts.
+__device__ void gather_issue(const BJob &j, uint32_t q, unsigned char *buf,
+                             uint32_t *rowoff, uint64_t *bar) {
+  const uint32_t lane = threadIdx.x & 31;
+  const GBlock k = gather_decode(j, q);
+  const uint32_t len = k.sj * j.b * j.e;
+  const uint64_t row_bytes = (uint64_t)j.row_elems * j.e;
+  const char *row0 = j.base + ((uint64_t)k.t * j.tile_elems +
+                               (uint64_t)k.i0 * j.row_elems +
+                               (uint64_t)k.j0 * j.b) * j.e;
+  uint32_t bytes = 0;
+  for (uint32_t r = lane; r < k.si; r += 32) {
+    const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
+    const uintptr_t a0 = src & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + len + 15) & ~(uintptr_t)15;
+    bytes += (uint32_t)(a1 - a0);
+    rowoff[r] = r * j.pitch + (uint32_t)(src - a0);
   }
-  __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+  fence_proxy_async_smem();
+  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+  __syncwarp();
+  for (uint32_t r = lane; r < k.si; r += 32) {
+    const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
+    const uintptr_t a0 = src & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + len + 15) & ~(uintptr_t)15;
+    bulk_g2s(buf + (size_t)r * j.pitch, (const void *)a0, (uint32_t)(a1 - a0),
+             bar);
+  }
+}
+
+// All threads: output rows j0..j0+sj-1 of the block, each si*b elements
+// long, from the staged rows.
+template <int E>
+__device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf,
+                             const uint32_t *rowoff) {
+  using T = typename Elem<E>::T;
+  const GBlock k = gather_decode(j, q);
+  T *dst = reinterpret_cast<T *>(j.scratch) + (uint64_t)k.t * j.tile_elems +
+           ((uint64_t)k.j0 * j.a + k.i0) * j.b;
+  if (j.b == 1) {
+    store_b1<E>(buf, rowoff, k.si, k.sj, j.ng8, j.div_ng8, dst, j.a,
+                threadIdx.x >> 5, kStageThreads / 32);
+    return;
+  }
+  const uint32_t ob = k.si * j.b;  // elements per output row segment
+  const uint32_t n = k.sj * ob;
+  const FastDiv div_ob = k.si == j.S ? j.div_Sb : make_fastdiv(ob);
+  const uint64_t ostride = (uint64_t)j.a * j.b;
   for (uint32_t base = threadIdx.x; base < n; base += kStageThreads * 4) {
     T v[4];
-    uint64_t go[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const uint32_t idx = base + u * kStageThreads;
-      const uint32_t jj = fdiv(idx, j.div_Sb);
-      const uint32_t rem = idx - jj * Sb;
-      go[u] = ~0ull;
-      if (idx < n && jj < sj && rem < lim_o) {
+      const uint32_t o = base + u * kStageThreads;
+      if (o < n) {
+        const uint32_t jj = fdiv(o, div_ob);
+        const uint32_t rem = o - jj * ob;
         uint32_t ii = rem, sub = 0;
         if (j.b != 1) {
           ii = fdiv(rem, j.div_b);
           sub = rem - ii * j.b;
         }
-        v[u] = *reinterpret_cast<const T *>(smem + ii * j.pitch +
+        v[u] = *reinterpret_cast<const T *>(buf + rowoff[ii] +
                                             (jj * j.b + sub) * E);
-        go[u] = (uint64_t)jj * j.a * j.b + rem;
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (go[u] != ~0ull) __stcg(dst + go[u], v[u]);
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t o = base + u * kStageThreads;
+      if (o < n) {
+        const uint32_t jj = fdiv(o, div_ob);
+        __stcg(dst + jj * ostride + (o - jj * ob), v[u]);
+      }
+    }
   }
-  __syncthreads();
 }
 
-__global__ void __launch_bounds__(kStageThreads) k_batch_gather(BatchArgs g) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t s_item;
-  while (true) {
-    if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
-    __syncthreads();
-    const uint32_t k = s_item;
-    __syncthreads();
-    if (k >= g.nitems) break;
-    const BItem it = g.items[k];
-    const BJob j = g.jobs[it.job];
-    for (uint32_t q = (uint32_t)it.tile0; q < (uint32_t)it.tile0 + it.ntiles; ++q) {
-      switch (j.e) {
-        case 1: gather_block<1>(j, q, smem); break;
-        case 2: gather_block<2>(j, q, smem); break;
-        case 4: gather_block<4>(j, q, smem); break;
-        default: gather_block<8>(j, q, smem); break;
+// Persistent: every CTA walks blocks (claimed item by item from the work
+// counter) with two shared-memory stages, loading block n+1 by bulk copies
+// while it writes block n.
+__global__ void __launch_bounds__(kStageThreads, 3) k_batch_gather(BatchArgs g) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t rowoff[2][kStageMaxS];
+  __shared__ uint32_t s_job[2], s_q[2], s_valid[2];
+  __shared__ int s_dead;
+  __shared__ __align__(16) BJob s_jobs[2];  // job of the block in each stage
+  const uint32_t warp = threadIdx.x >> 5;
+  uint32_t c_job = 0, c_q = 0, c_end = 0;  // thread 0's cursor
+  auto fetch = [&](int slot) {
+    if (c_q >= c_end) {
+      const uint32_t k = atomicAdd(g.counter, 1u);
+      if (k >= g.nitems) {
+        s_valid[slot] = 0;
+        return;
       }
+      const BItem it = g.items[k];
+      c_job = it.job;
+      c_q = (uint32_t)it.tile0;
+      c_end = c_q + it.ntiles;
+    }
+    s_job[slot] = c_job;
+    s_q[slot] = c_q++;
+    s_valid[slot] = 1;
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    s_dead = 0;
+    fetch(0);
+  }
+  __syncthreads();
+  if (!s_valid[0]) return;
+  uint32_t cq = s_q[0];
+  if (warp == 0) {
+    copy_job(&s_jobs[0], &g.jobs[s_job[0]]);
+    gather_issue(g.jobs[s_job[0]], cq, smem, rowoff[0], &bar[0]);
+  }
+  uint32_t parity = 0;   // bit st: phase to wait for on bar[st]
+  uint32_t pending = 1;  // bit st: loads issued to stage st, not yet seen
+
+  for (uint32_t n = 0;; ++n) {
+    const int st = n & 1, nx = st ^ 1;
+    if (threadIdx.x == 0) fetch(nx);
+    __syncthreads();  // slot nx visible; stage nx free since the last pass
+    const bool more = s_valid[nx] != 0 && !s_dead;
+    const uint32_t nj = s_job[nx], nq = s_q[nx];
+    if (more) {
+      if (warp == 0) {
+        copy_job(&s_jobs[nx], &g.jobs[nj]);
+        gather_issue(g.jobs[nj], nq, smem + (size_t)nx * g.stage_bytes,
+                     rowoff[nx], &bar[nx]);
+      }
+      pending |= 1u << nx;
+    }
+    // wait for block n (bounded; a load that never lands stops this CTA)
+    const uint64_t t0 = global_timer_ns();
+    bool landed = true;
+    while (!mbar_try_wait(&bar[st], (parity >> st) & 1))
+      if (global_timer_ns() - t0 > 2000000000ull) {
+        landed = false;
+        break;
+      }
+    if (landed) {
+      parity ^= 1u << st;
+      pending &= ~(1u << st);
+      const BJob &j = s_jobs[st];
+      const unsigned char *buf = smem + (size_t)st * g.stage_bytes;
+      switch (j.e) {
+        case 1: gather_store<1>(j, cq, buf, rowoff[st]); break;
+        case 2: gather_store<2>(j, cq, buf, rowoff[st]); break;
+        case 4: gather_store<4>(j, cq, buf, rowoff[st]); break;
+        default: gather_store<8>(j, cq, buf, rowoff[st]); break;
+      }
+    } else {
+      s_dead = 1;
+      if (g.status) atomicExch(g.status, kStatusWaitTimeout);
+    }
+    __syncthreads();  // stage st read by everyone; slot nx read by everyone
+    if (!more || s_dead) break;
+    cq = nq;
+  }
+  // nothing may still be landing in shared memory when the CTA exits
+  for (int st = 0; st < 2; ++st) {
+    if (!((pending >> st) & 1)) continue;
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(&bar[st], (parity >> st) & 1) &&
+           global_timer_ns() - t0 < 2000000000ull) {
     }
   }
 }
@@ -393,24 +626,26 @@ __global__ void __launch_bounds__(kStageThreads) k_batch_copyback(BatchArgs g) {
 // ---- host -------------------------------------------------------------------
 
 // Cluster form of one tile of a x (B*b) elements of e bytes: the smallest
-// cluster (2..16 CTAs) whose column bands fit `budget` bytes of shared memory
-// each, preferring bands small enough for two CTAs per SM and clusters of at
-// most 8.  Returns the group index (log2(C) - 1) or -1.
+// cluster (2..16 CTAs) whose column bands fit `half` bytes (a stage size
+// that leaves room for two CTAs per SM), else the smallest whose bands fit
+// `budget` bytes (one of the two shared-memory stages of a CTA).  Returns the
+// group index (log2(C) - 1) or -1.
 static int band_group(uint64_t a, uint64_t B, uint64_t b, int e, size_t budget,
-                      uint32_t *band, uint32_t *pitch) {
+                      size_t half, uint32_t *band, uint32_t *pitch,
+                      bool *two_per_sm) {
   if (a > kBandMaxRows || a * B * b >= 0xffffffffull) return -1;
-  const size_t half = budget / 2 - 1024;
   for (int pass = 0; pass < 2; ++pass) {
     for (int gi = 0; gi < kBandGroups; ++gi) {
       const uint64_t C = 2ull << gi;
-      if (pass == 0 && C > 8) break;
       const uint64_t bd = (B + C - 1) / C;
       // a 16-byte aligned superset of a row segment of len bytes spans at
       // most round16(len) + 16 bytes
-      const uint64_t bp = (bd * b * e + 15) / 16 * 16 + 16;
+      uint64_t bp = (bd * b * e + 15) / 16 * 16 + 16;
+      if (((bp / 16) & 1) == 0) bp += 16;  // rows in distinct bank groups
       if (bp * a <= (pass == 0 ? half : budget)) {
         *band = (uint32_t)bd;
         *pitch = (uint32_t)bp;
+        *two_per_sm = pass == 0;
         return gi;
       }
     }
@@ -502,9 +737,9 @@ struct lm_batch_st {
   uint64_t gkey = 0;
   void *h_gstage = nullptr;  // pinned copy of the job table owned by gexec
   cudaEvent_t uploaded = nullptr;  // last upload from h_stage
-  cudaStream_t side[lm::kSideStreams] = {};  // large jobs run here
+  cudaStream_t side[lm::kSideStreams] = {};  // large jobs and groups run here
   cudaEvent_t join[lm::kSideStreams] = {};
-  cudaEvent_t fork = nullptr;
+  cudaEvent_t fork = nullptr, fork2 = nullptr;
   uint64_t seen_key = 0;  // job list of the previous graph-mode run
   // last run statistics
   lm_batch_stats stats;
@@ -605,6 +840,8 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.div_aB = make_fastdiv(j.aB);
   j.div_a = make_fastdiv(j.a);
   j.band = 0;
+  j.ng8 = (uint32_t)((nz.a + 7) / 8);
+  j.div_ng8 = make_fastdiv(j.ng8);
   j.scratch = nullptr;
   j.S = j.nJ = j.nIJ = 0;
   j.bytes = 0;
@@ -616,9 +853,14 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
                        unsigned flags) {
   const DeviceInfo &di = device_info();
   const uint64_t max_tile = (uint64_t)di.max_smem_optin - 1024;
-  // dynamic shared memory left to the cluster kernel beside its row table
+  // one of the cluster kernel's two stages, beside its row tables
+  const size_t band_static = 2 * kBandMaxRows * 4 + 512;
   const size_t band_budget =
-      (size_t)di.max_smem_optin - (kBandMaxRows * 4 + 512);
+      ((size_t)di.max_smem_optin - band_static) / 2 / 128 * 128;
+  // ... and the stage size that lets two CTAs share an SM (each also holds
+  // 1 KB of shared memory reserved by the system)
+  const size_t band_half =
+      ((size_t)di.max_smem_per_sm / 2 - 1024 - band_static) / 2 / 128 * 128;
   bt->jobs.clear();
   bt->small.clear();
   bt->big.clear();
@@ -674,12 +916,21 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
     const uint64_t tile_elems = row_elems * nz.a;
     const uint32_t pitch = batch_pitch(row_elems * jb.elem_bytes, jb.elem_bytes);
     const uint64_t tile_smem = (uint64_t)pitch * nz.a;
-    if (tile_elems >= 0xffffffffull || tile_smem > max_tile) {
+    if (tile_elems >= 0xffffffffull || tile_smem > kSmallItem) {
       uint32_t band = 0, bpitch = 0;
-      const int gi = (flags & LM_BATCH_NO_CLUSTER)
-                         ? -1
-                         : band_group(nz.a, nz.B, nz.b, jb.elem_bytes,
-                                      band_budget, &band, &bpitch);
+      bool two_per_sm = false;
+      int gi = (flags & LM_BATCH_NO_CLUSTER)
+                   ? -1
+                   : band_group(nz.a, nz.B, nz.b, jb.elem_bytes, band_budget,
+                                band_half, &band, &bpitch, &two_per_sm);
+      const uint64_t unit = nz.b * (uint64_t)jb.elem_bytes;
+      const uint64_t foot = (bytes + 255) / 256 * 256 + 256;
+      const bool stageable = foot <= arena_cap && unit <= kStageTileBytes &&
+                             tile_elems < 0xffffffffull;
+      // clusters of 8 or 16 CTAs, one per SM, leave a fifth of the SMs idle
+      // (whole clusters per GPC) and hold little in flight per CTA: the
+      // staged form moves such tiles faster
+      if (gi >= 2 && !two_per_sm && stageable) gi = -1;
       if (gi >= 0) {
         BJob j;
         fill_job(j, jb, nz, bpitch);
@@ -693,17 +944,31 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
           it.ntiles = 1;
           bt->band[gi].push_back(it);
         }
-        bt->band_smem[gi] =
-            std::max<size_t>(bt->band_smem[gi], (size_t)bpitch * nz.a);
+        bt->band_smem[gi] = std::max<size_t>(
+            bt->band_smem[gi], ((size_t)bpitch * nz.a + 127) / 128 * 128);
         bt->stats.band_jobs += 1;
         bt->stats.band_bytes += bytes;
         continue;
       }
+      if (tile_elems < 0xffffffffull && tile_smem <= max_tile) {
+        // one CTA per tile (more than kBandMaxRows rows, or no clusters)
+        BJob j;
+        fill_job(j, jb, nz, pitch);
+        const uint32_t jid = (uint32_t)bt->jobs.size();
+        bt->jobs.push_back(j);
+        for (uint64_t t0 = 0; t0 < nz.T; ++t0) {
+          BItem it;
+          it.job = jid;
+          it.tile0 = t0;
+          it.ntiles = 1;
+          bt->big.push_back(it);
+        }
+        bt->stats.big_jobs += 1;
+        bt->stats.big_bytes += bytes;
+        continue;
+      }
       // staged: the job fits the arena (in the current wave or a new one)
-      const uint64_t unit = nz.b * (uint64_t)jb.elem_bytes;
-      const uint64_t foot = (bytes + 255) / 256 * 256 + 256;
-      if (foot <= arena_cap && unit <= kStageTileBytes &&
-          tile_elems < 0xffffffffull) {
+      if (stageable) {
         if (bt->nwaves == 0 || wave_used + foot > arena_cap) {
           if (bt->nwaves == kMaxWaves) goto planner;
           bt->nwaves += 1;
@@ -716,9 +981,13 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
           const uint64_t nI = (nz.a + S - 1) / S, nJ = (nz.B + S - 1) / S;
           if (nz.T * nI * nJ >= 0xffffffffull) goto planner;
           BJob j;
-          const uint32_t sp = batch_pitch((uint64_t)S * unit, jb.elem_bytes);
+          // staged rows: 16-byte aligned supersets of S-unit segments
+          uint32_t sp = (uint32_t)((S * unit + 15) / 16 * 16 + 16);
+          if (((sp / 16) & 1) == 0) sp += 16;  // rows in distinct bank groups
           fill_job(j, jb, nz, sp);
           j.S = S;
+          j.ng8 = (S + 7) / 8;
+          j.div_ng8 = make_fastdiv(j.ng8);
           j.nJ = (uint32_t)nJ;
           j.nIJ = (uint32_t)(nI * nJ);
           j.div_Sb = make_fastdiv(S * (uint32_t)nz.b);
@@ -746,7 +1015,8 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
             it.ntiles = 0;
             bt->wcopy[w].push_back(it);
           }
-          bt->wsmem[w] = std::max<size_t>(bt->wsmem[w], (size_t)S * sp);
+          bt->wsmem[w] =
+              std::max<size_t>(bt->wsmem[w], ((size_t)S * sp + 127) / 128 * 128);
           wave_used += foot;
           bt->need_arena = std::max(bt->need_arena, wave_used);
           bt->stats.staged_jobs += 1;
@@ -764,29 +1034,17 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
     fill_job(j, jb, nz, pitch);
     const uint32_t jid = (uint32_t)bt->jobs.size();
     bt->jobs.push_back(j);
-    if (tile_smem <= kSmallItem) {
-      uint64_t k_t = std::max<uint64_t>(1, kSmallItem / tile_smem);
-      while (k_t > 1 && k_t * tile_elems >= 0xffffffffull) --k_t;
-      for (uint64_t t0 = 0; t0 < nz.T; t0 += k_t) {
-        BItem it;
-        it.job = jid;
-        it.tile0 = t0;
-        it.ntiles = (uint32_t)std::min<uint64_t>(k_t, nz.T - t0);
-        bt->small.push_back(it);
-      }
-      bt->stats.small_jobs += 1;
-      bt->stats.small_bytes += bytes;
-    } else {
-      for (uint64_t t0 = 0; t0 < nz.T; ++t0) {
-        BItem it;
-        it.job = jid;
-        it.tile0 = t0;
-        it.ntiles = 1;
-        bt->big.push_back(it);
-      }
-      bt->stats.big_jobs += 1;
-      bt->stats.big_bytes += bytes;
+    uint64_t k_t = std::max<uint64_t>(1, kSmallItem / tile_smem);
+    while (k_t > 1 && k_t * tile_elems >= 0xffffffffull) --k_t;
+    for (uint64_t t0 = 0; t0 < nz.T; t0 += k_t) {
+      BItem it;
+      it.job = jid;
+      it.tile0 = t0;
+      it.ntiles = (uint32_t)std::min<uint64_t>(k_t, nz.T - t0);
+      bt->small.push_back(it);
     }
+    bt->stats.small_jobs += 1;
+    bt->stats.small_bytes += bytes;
   }
   bt->stats.small_items = bt->small.size();
   bt->stats.big_items = bt->big.size();
@@ -800,8 +1058,9 @@ static bool launch_band(cudaStream_t s, const BJob *d_jobs,
                         const BItem *d_items, uint32_t nitems,
                         uint32_t *counter, size_t smem, int C) {
   if (nitems == 0) return false;
+  const size_t dyn = 2 * smem;  // two stages
   cudaError_t err = cudaFuncSetAttribute(
-      k_batch_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_batch_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   if (err == cudaSuccess && C > 8)
     err = cudaFuncSetAttribute(k_batch_band,
                                cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -814,7 +1073,7 @@ static bool launch_band(cudaStream_t s, const BJob *d_jobs,
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(kBatchThreads);
-  cfg.dynamicSmemBytes = smem;
+  cfg.dynamicSmemBytes = dyn;
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
@@ -831,6 +1090,7 @@ static bool launch_band(cudaStream_t s, const BJob *d_jobs,
   g.nitems = nitems;
   g.counter = counter;
   g.status = device_status_word();
+  g.stage_bytes = (uint32_t)smem;
   if (getenv("LM_VERBOSE"))
     fprintf(stderr, "batch_band: C=%d smem=%zu items=%u clusters=%llu\n", C,
             smem, nitems, (unsigned long long)ncl);
@@ -847,13 +1107,15 @@ static bool launch_staged(cudaStream_t s, const BJob *d_jobs,
   if (nitems == 0) return false;
   const DeviceInfo &di = device_info();
   auto kern = copyback ? k_batch_copyback : k_batch_gather;
-  if (smem > 48 * 1024 &&
+  // the gather keeps two stages of `smem` bytes
+  const size_t dyn = copyback ? 0 : 2 * smem;
+  if (dyn > 48 * 1024 &&
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
+                           (int)dyn) != cudaSuccess)
     return set_error("batch: smem attribute");
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kStageThreads,
-                                                    smem) != cudaSuccess ||
+                                                    dyn) != cudaSuccess ||
       occ < 1)
     return set_error("batch: occupancy");
   const uint32_t grid =
@@ -863,9 +1125,10 @@ static bool launch_staged(cudaStream_t s, const BJob *d_jobs,
   g.items = d_items;
   g.nitems = nitems;
   g.counter = counter;
-  g.status = nullptr;
+  g.status = device_status_word();
+  g.stage_bytes = (uint32_t)smem;
   ProfScope ps(s, copyback ? "batch_copyback" : "batch_gather");
-  kern<<<grid, kStageThreads, smem, s>>>(g);
+  kern<<<grid, kStageThreads, dyn, s>>>(g);
   if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
   return false;
 }
@@ -913,7 +1176,10 @@ static size_t stage_bytes(lm_batch_t bt) {
 // the batch's stream (both work under stream capture).
 static bool ensure_side(lm_batch_t bt) {
   if (bt->fork) return false;
-  if (cudaEventCreateWithFlags(&bt->fork, cudaEventDisableTiming) != cudaSuccess)
+  if (cudaEventCreateWithFlags(&bt->fork, cudaEventDisableTiming) !=
+          cudaSuccess ||
+      cudaEventCreateWithFlags(&bt->fork2, cudaEventDisableTiming) !=
+          cudaSuccess)
     return set_error("batch: fork event");
   for (int k = 0; k < kSideStreams; ++k) {
     if (cudaStreamCreateWithFlags(&bt->side[k], cudaStreamNonBlocking) !=
@@ -926,9 +1192,10 @@ static bool ensure_side(lm_batch_t bt) {
 }
 
 // Large jobs, longest first, each on the side stream with the least work so
-// far (greedy longest-processing-time order).
+// far (greedy longest-processing-time order).  Sets a bit in *used for every
+// side stream it forks; the caller joins them.
 static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
-                          unsigned flags) {
+                          unsigned flags, unsigned *used) {
   if (bt->large.empty()) return false;
   std::vector<uint32_t> order(bt->large);
   auto bytes_of = [&](uint32_t k) {
@@ -942,7 +1209,10 @@ static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   if (nside > 1 && ensure_side(bt)) return true;
   if (nside > 1) {
     cudaEventRecord(bt->fork, s);
-    for (int k = 0; k < nside; ++k) cudaStreamWaitEvent(bt->side[k], bt->fork, 0);
+    for (int k = 0; k < nside; ++k) {
+      cudaStreamWaitEvent(bt->side[k], bt->fork, 0);
+      *used |= 1u << k;
+    }
   }
   uint64_t load[kSideStreams] = {};
   for (uint32_t k : order) {
@@ -956,12 +1226,6 @@ static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
                          nz.B, nz.b, (flags & LM_BATCH_NO_TUNE) ? 0 : 1))
       return true;
   }
-  if (nside > 1) {
-    for (int k = 0; k < nside; ++k) {
-      cudaEventRecord(bt->join[k], bt->side[k]);
-      cudaStreamWaitEvent(s, bt->join[k], 0);
-    }
-  }
   return false;
 }
 
@@ -974,7 +1238,8 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   const size_t ni = item_count(bt);
   if (grow(bt, std::max<size_t>(nj, 1), std::max<size_t>(ni, 1))) return true;
   // the large jobs need no table: they start first, on the side streams
-  if (enqueue_large(bt, s, jobs, flags)) return true;
+  unsigned used = 0;
+  if (enqueue_large(bt, s, jobs, flags, &used)) return true;
   // stage: jobs, then small items, big items and the cluster groups.  The
   // shared staging buffer is reused only after the previous upload from it
   // has executed.
@@ -1017,37 +1282,78 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   }
   if (cudaMemsetAsync(bt->d_counters, 0, kCounterBytes, s) != cudaSuccess)
     return set_error("batch: counter clear");
-  if (launch_items(s, bt->d_jobs, bt->d_items, (uint32_t)bt->small.size(),
-                   bt->d_counters, kSmallItem + 256))
-    return true;
-  size_t off = bt->small.size();
-  if (!bt->big.empty()) {
-    const DeviceInfo &di = device_info();
-    if (launch_items(s, bt->d_jobs, bt->d_items + off,
-                     (uint32_t)bt->big.size(), bt->d_counters + kCounterStride,
-                     (size_t)di.max_smem_optin - 1024))
-      return true;
-  }
-  off += bt->big.size();
+  // The groups are independent: the staged waves (in order, they share the
+  // arena), each cluster size and the one-CTA items run on their own
+  // streams, forked here from `s` and joined back at the end, so that one
+  // persistent kernel's tail overlaps the others.
+  const size_t off_big = bt->small.size();
+  size_t off_band[kBandGroups];
+  size_t off = off_big + bt->big.size();
   for (int gi = 0; gi < kBandGroups; ++gi) {
-    if (launch_band(s, bt->d_jobs, bt->d_items + off,
+    off_band[gi] = off;
+    off += bt->band[gi].size();
+  }
+  const size_t off_waves = off;
+  int nq = 0;
+  cudaStream_t q[1 + kBandGroups + 1];
+  int ngroups = (bt->nwaves > 0) + (!bt->small.empty() || !bt->big.empty());
+  for (int gi = 0; gi < kBandGroups; ++gi) ngroups += !bt->band[gi].empty();
+  if (ngroups > 1) {
+    if (ensure_side(bt)) return true;
+    cudaEventRecord(bt->fork2, s);  // tables uploaded, counters cleared
+  }
+  auto next_stream = [&]() -> cudaStream_t {
+    // the first group runs on s itself
+    if (nq == 0) return q[nq++] = s;
+    cudaStream_t side = bt->side[nq - 1];
+    cudaStreamWaitEvent(side, bt->fork2, 0);
+    used |= 1u << (nq - 1);
+    return q[nq++] = side;
+  };
+  if (bt->nwaves > 0) {
+    const cudaStream_t ws = next_stream();
+    off = off_waves;
+    for (int w = 0; w < bt->nwaves; ++w) {
+      uint32_t *c = bt->d_counters + (2 + kBandGroups + 2 * w) * kCounterStride;
+      if (launch_staged(ws, bt->d_jobs, bt->d_items + off,
+                        (uint32_t)bt->wgather[w].size(), c, bt->wsmem[w],
+                        false))
+        return true;
+      off += bt->wgather[w].size();
+      if (launch_staged(ws, bt->d_jobs, bt->d_items + off,
+                        (uint32_t)bt->wcopy[w].size(), c + kCounterStride, 0,
+                        true))
+        return true;
+      off += bt->wcopy[w].size();
+    }
+  }
+  for (int gi = kBandGroups - 1; gi >= 0; --gi) {
+    if (bt->band[gi].empty()) continue;
+    const cudaStream_t bs = next_stream();
+    if (launch_band(bs, bt->d_jobs, bt->d_items + off_band[gi],
                     (uint32_t)bt->band[gi].size(),
                     bt->d_counters + (2 + gi) * kCounterStride,
                     bt->band_smem[gi], 2 << gi))
       return true;
-    off += bt->band[gi].size();
   }
-  for (int w = 0; w < bt->nwaves; ++w) {
-    uint32_t *c = bt->d_counters + (2 + kBandGroups + 2 * w) * kCounterStride;
-    if (launch_staged(s, bt->d_jobs, bt->d_items + off,
-                      (uint32_t)bt->wgather[w].size(), c, bt->wsmem[w], false))
+  if (!bt->small.empty() || !bt->big.empty()) {
+    const cudaStream_t ts = next_stream();
+    if (launch_items(ts, bt->d_jobs, bt->d_items, (uint32_t)bt->small.size(),
+                     bt->d_counters, kSmallItem + 256))
       return true;
-    off += bt->wgather[w].size();
-    if (launch_staged(s, bt->d_jobs, bt->d_items + off,
-                      (uint32_t)bt->wcopy[w].size(), c + kCounterStride, 0,
-                      true))
-      return true;
-    off += bt->wcopy[w].size();
+    if (!bt->big.empty()) {
+      const DeviceInfo &di = device_info();
+      if (launch_items(ts, bt->d_jobs, bt->d_items + off_big,
+                       (uint32_t)bt->big.size(),
+                       bt->d_counters + kCounterStride,
+                       (size_t)di.max_smem_optin - 1024))
+        return true;
+    }
+  }
+  for (int k = 0; k < kSideStreams; ++k) {
+    if (!((used >> k) & 1)) continue;
+    cudaEventRecord(bt->join[k], bt->side[k]);
+    cudaStreamWaitEvent(s, bt->join[k], 0);
   }
   return false;
 }
@@ -1077,6 +1383,7 @@ void lm_batch_destroy(lm_batch_t bt) {
     if (bt->join[k]) cudaEventDestroy(bt->join[k]);
   }
   if (bt->fork) cudaEventDestroy(bt->fork);
+  if (bt->fork2) cudaEventDestroy(bt->fork2);
   delete bt;
 }
 

@@ -163,6 +163,19 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
       : "memory");
 }
 
+// Cluster barrier halves.  A relaxed arrive orders no memory accesses (use it
+// where the barrier only has to order execution); the default arrive has
+// release semantics and the wait acquire semantics, at cluster scope.
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Status word written by kernels that wait on other CTAs; the host turns a
 // non-zero value into an error return.
 enum : uint32_t {

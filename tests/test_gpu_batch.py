@@ -147,28 +147,31 @@ def test_batch_rejects_bad_jobs(cuda):
     bt.close()
 
 
-# Tiles too large for one CTA's shared memory but small enough for a cluster
-# of 2..16 CTAs (column bands of at most ~222 KB each), with odd, unaligned
-# row lengths and every element width.
+# Tiles too large for one CTA's shared memory tile budget (40 KB) but small
+# enough for a cluster of 2..16 CTAs (two stages of column bands of at most
+# ~109 KB each), with odd, unaligned row lengths and every element width.
 BAND_SPECS = [
-    (7, (256, 300), 4),                 # clusters of 4
-    (7, (333, 777), 2),                 # unaligned rows, clusters of 8
-    (3, (64 * 7, 3000, 64), 8),         # 7 tiles of 64 x 3000
+    (7, (256, 300), 4),                 # clusters of 8, two CTAs per SM
+    (7, (333, 777), 2),                 # unaligned rows
+    (3, (64 * 7, 3000, 64), 8),         # 7 tiles of 64 x 3000, clusters of 16
     (2, (500, 999, 3), 1),              # b = 3, bytes
-    (7, (600, 700), 4),                 # one CTA per SM per band
-    (7, (1000, 800), 4),                # clusters of 16
+    (7, (600, 350), 4),
+    (7, (1000, 300), 4),                # 1000 rows
     (0, (5, 100, 2000, 1), 4),          # 5 tiles
-    (0, (3, 200, 300, 5), 8),           # b = 5, 8-byte elements
+    (0, (3, 200, 150, 5), 8),           # b = 5, 8-byte elements
     (4, (64 * 5, 1000, 64), 8),         # ASTA -> AoS, 1000-row tiles
 ]
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_batch_cluster_items(cuda, graph):
+@pytest.mark.parametrize("graph,scratch", [(False, False), (True, False),
+                                           (True, True)])
+def test_batch_cluster_items(cuda, graph, scratch):
     specs = make_jobs(3, 40, 16, 200, big=BAND_SPECS)
-    st = run_and_check(cuda, specs, graph=graph, reps=3 if graph else 1)
-    assert st["band_jobs"] == len(BAND_SPECS), st
-    assert st["band_items"] >= st["band_jobs"]
+    st = run_and_check(cuda, specs, graph=graph, reps=3 if graph else 1,
+                       scratch=scratch)
+    if not scratch:  # every cluster size, one and two CTAs per SM
+        assert st["band_jobs"] >= len(BAND_SPECS), st
+    assert st["band_items"] >= st["band_jobs"] > 0
 
 
 def test_batch_cluster_off_matches(cuda):
