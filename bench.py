@@ -487,6 +487,132 @@ def run_batch_workload(args, ws, rank, local):
     return 0
 
 
+
+# ---- served workload (Poisson arrivals, continuous batching) -----------------
+
+SERVE_OPS = ("aos_asta", "asta_aos", "soa_asta", "asta_soa", "transpose")
+
+
+def serve_trace(n, rate, seed=2, lo=4 << 10, hi=512 << 20):
+    """n requests with Poisson arrivals at `rate` per second (seed 2),
+    payload log-uniform in [4 KiB, 512 MiB], element width uniform in
+    {1, 2, 4, 8}, op uniform over the layout conversions (AoS<->ASTA and
+    SoA<->ASTA with tile t in {16, 32, 64} and 2..1024 fields, and the full
+    transpose)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=n)
+    arrival = np.cumsum(gaps) - gaps[0]
+    out = []
+    for k in range(n):
+        e = int(rng.choice([1, 2, 4, 8]))
+        nel = max(64, int(np.exp(rng.uniform(np.log(lo), np.log(hi)))) // e)
+        op = SERVE_OPS[int(rng.integers(0, len(SERVE_OPS)))]
+        t = int(rng.choice([16, 32, 64]))
+        if op == "transpose":
+            m = int(np.exp(rng.uniform(np.log(16), np.log(max(17, nel // 16)))))
+            dims = (m, max(1, nel // m))
+        else:
+            w = int(np.exp(rng.uniform(np.log(2), np.log(1024))))
+            h = max(t, (nel // w) // t * t)
+            dims = (h, w, t)
+        out.append((int(arrival[k] * 1e9), op, dims, e))
+    return out
+
+
+def run_serve_workload(args, ws, rank, local):
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from libmarshal_gb300 import lm
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    code = {"aos_asta": lm.OP_AOS_ASTA, "asta_aos": lm.OP_ASTA_AOS,
+            "soa_asta": lm.OP_SOA_ASTA, "asta_soa": lm.OP_ASTA_SOA,
+            "transpose": lm.OP_TRANSPOSE}
+    budget = 120 << 30
+    free, _ = torch.cuda.mem_get_info(dev)
+    ring = min(budget, int(free * 0.45)) // 256 * 256
+    arena = torch.empty(ring // 8, dtype=torch.int64, device=dev)
+    arena.random_(generator=torch.Generator(device=dev).manual_seed(7))
+    base = arena.data_ptr()
+    results = []
+    for rate in args.serve_rates:
+        trace = serve_trace(args.serve_n, rate)
+        reqs, arrival, after, spans, payload = [], [], [], [], 0
+        off = 0
+        for k, (t_ns, op, dims, e) in enumerate(trace):
+            nbytes = dims[0] * dims[1] * e  # h x w (or M x N) elements
+            size = (nbytes + 255) // 256 * 256
+            if off + size > ring:
+                off = 0
+            # ring reuse: wait for every earlier request on these bytes
+            dep = -1
+            for j in range(k - 1, -1, -1):
+                s0, s1 = spans[j]
+                if s0 < off + size and off < s1:
+                    dep = j
+                    break
+            spans.append((off, off + size))
+            d = list(dims) + [0] * (4 - len(dims))
+            r = lm.Request()
+            r.elem_bytes, r.op = e, code[op]
+            r.d0, r.d1, r.d2, r.d3 = d
+            r.buf = base + off
+            reqs.append(r)
+            arrival.append(t_ns)
+            after.append(dep)
+            payload += nbytes
+            off += size
+        row = {"rate_per_s": rate, "requests": len(reqs),
+               "payload_bytes": payload}
+        for mode in ("served", "plain"):
+            torch.cuda.synchronize()
+            srv = None if mode == "plain" else lm.Server(budget)
+            res = lm.serve_replay(srv, reqs, arrival, after,
+                                  plain=(mode == "plain"))
+            st = srv.stats() if srv is not None else None
+            if srv is not None:
+                srv.close()
+            if any(r[0] for r in res):
+                raise RuntimeError("a %s request failed" % mode)
+            lat = np.array([r[1] for r in res], dtype=np.float64) / 1e6
+            done_last = max(a + r[1] for a, r in zip(arrival, res))
+            span_s = (done_last - arrival[0]) / 1e9
+            row[mode] = {
+                "GBps": round(2.0 * payload / span_s / 1e9, 2),
+                "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                "max_ms": round(float(lat.max()), 3),
+                "mean_queue_ms": round(float(np.mean([r[2] for r in res]))
+                                       / 1e6, 3),
+                "makespan_ms": round(span_s * 1e3, 2)}
+            if st is not None:
+                row[mode]["batches"] = st["batches"]
+                row[mode]["peak_inflight_GB"] = round(
+                    st["peak_inflight_bytes"] / 1e9, 2)
+        results.append(row)
+    peak, peak_kind = peak_hbm()
+    top = results[-1]
+    line = {
+        "metric": "served_conversion_GBps", "value": top["served"]["GBps"],
+        "unit": "GB/s", "n_gpus": ws, "steps": len(results),
+        "warmup": 0, "ms_per_step": top["served"]["makespan_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "mixed u8/u16/u32/u64",
+        "data": "synthetic (seeded random bits, Poisson arrivals seed 2)",
+        "config": {"workload": "serve_poisson_4KiB_512MiB",
+                   "budget_bytes": budget, "ring_bytes": ring,
+                   "requests_per_rate": args.serve_n,
+                   "rates_per_s": list(args.serve_rates)},
+        "p50_ms": top["served"]["p50_ms"], "p99_ms": top["served"]["p99_ms"],
+        "peak": peak, "peak_kind": peak_kind, "rates": results,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -501,6 +627,11 @@ def main():
                     help="matrices in the batched workload")
     ap.add_argument("--skip-plain", action="store_true",
                     help="batched workload: skip the per-request loop")
+    ap.add_argument("--serve-n", type=int, default=2000,
+                    help="requests per arrival rate in the served workload")
+    ap.add_argument("--serve-rates", type=float, nargs="+",
+                    default=[1000.0, 10000.0, 100000.0],
+                    help="Poisson arrival rates (requests/s)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -511,6 +642,8 @@ def main():
     ws, rank, local = dist_setup(args.gpus)
     if args.workload == "batch":
         return run_batch_workload(args, ws, rank, local)
+    if args.workload == "serve":
+        return run_serve_workload(args, ws, rank, local)
     return run_ours(args, ws, rank, local)
 
 

@@ -206,6 +206,58 @@ bool lm_batch_stats_get(lm_batch_t batch, lm_batch_stats *out);
 /* Autotuner table: entries tuned so far (and loaded from LM_TUNE_FILE). */
 int lm_tune_entries(void);
 
+/* ---- conversion server (no reference counterpart) -------------------------
+ * lm_serve_create starts a worker thread on the current device.  Each
+ * lm_serve_submit queues one request; requests are admitted in submission
+ * order while the payload of admitted, unfinished requests stays within
+ * `budget_bytes`, sorted by payload into three lanes (<= 2 MiB, <= 64 MiB,
+ * larger) with their own prioritised streams, and run as batches
+ * (lm_batch_run) whenever a lane has a free slot.  A request on a device
+ * buffer (`buf`) is converted in place; with buf == NULL the host array
+ * `src` is copied to a device pool of budget_bytes, converted, and copied
+ * back to `dst` (which may equal src).  The caller keeps every buffer alive
+ * and untouched until the request's completion is polled.  lm_serve_poll
+ * returns up to cap completions (ticket, status 0 = ok, latency from
+ * submission to completion and time spent waiting for admission), or -1 on
+ * bad arguments. */
+typedef struct {
+  int elem_bytes; /* 1, 2, 4 or 8 */
+  int op;         /* LM_OP_* */
+  long long d0, d1, d2, d3;
+  void *buf;       /* device buffer converted in place, or NULL */
+  const void *src; /* host input when buf == NULL */
+  void *dst;       /* host output when buf == NULL */
+} lm_request;
+typedef struct {
+  unsigned long long ticket;
+  int status;
+  long long latency_ns, queue_ns;
+  long long done_ns; /* completion time, CLOCK_MONOTONIC nanoseconds */
+} lm_serve_done;
+typedef struct {
+  unsigned long long submitted, completed, batches, bytes, peak_inflight_bytes;
+} lm_serve_stats;
+typedef struct lm_serve_st *lm_serve_t;
+bool lm_serve_create(lm_serve_t *out, unsigned long long budget_bytes);
+bool lm_serve_submit(lm_serve_t server, const lm_request *req,
+                     unsigned long long *ticket);
+int lm_serve_poll(lm_serve_t server, lm_serve_done *out, int cap);
+/* Waits until every submitted request has completed (timeout_ms < 0: no
+ * limit); true on timeout or if a batch failed (lm_last_error says why). */
+bool lm_serve_drain(lm_serve_t server, long long timeout_ms);
+bool lm_serve_stats_get(lm_serve_t server, lm_serve_stats *out);
+void lm_serve_destroy(lm_serve_t server);
+/* Trace replay (load generator): request k is submitted arrival_ns[k] after
+ * the call starts, and not before requests 0..after[k] (-1: none; after[k]
+ * must be < k) have all completed, so a trace can reuse buffers ring-wise.  out[k] receives request k's
+ * completion, latency and queueing measured from its scheduled arrival.
+ * With LM_SERVE_PLAIN (server may be NULL) each request instead runs alone
+ * through the per-op planner on one stream at its arrival. */
+enum { LM_SERVE_PLAIN = 1 };
+bool lm_serve_replay(lm_serve_t server, const lm_request *reqs,
+                     const long long *arrival_ns, const int *after, int n,
+                     unsigned flags, lm_serve_done *out);
+
 /* ---- profiling (counterpart of include/cl_profile.h:6-63) ----------------
  * lm_launch_count: kernels launched by this library since it was loaded.
  * lm_prof_enable(1): from now on every launch is bracketed by a CUDA event

@@ -709,6 +709,22 @@ static Normalized normalize(const lm_job &jb) {
   return n;
 }
 
+bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
+                uint64_t *T, uint64_t *a, uint64_t *B, uint64_t *b) {
+  lm_job jb{};
+  jb.op = op;
+  jb.d0 = d0;
+  jb.d1 = d1;
+  jb.d2 = d2;
+  jb.d3 = d3;
+  const Normalized n = normalize(jb);
+  *T = n.T;
+  *a = n.a;
+  *B = n.B;
+  *b = n.b;
+  return n.ok;
+}
+
 }  // namespace lm
 
 struct lm_batch_st {

@@ -100,6 +100,11 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
 
 // The per-op planner (lm_api.cu) for one 0100; tune != 0 lets the
 // autotuner pick the algorithm of this shape class.
+// An LM_OP_* with its dimensions as the 0100(T, a, B, b) it performs; false
+// for an unknown op or bad dimensions (lm_batch.cu).
+bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
+                uint64_t *T, uint64_t *a, uint64_t *B, uint64_t *b);
+
 bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
                       uint64_t a, uint64_t B, uint64_t b, int tune);
 

@@ -57,6 +57,13 @@ _SIGS = {
     "lm_batch_run": (_B, [_VP, _VP, _VP, _I, ctypes.c_uint]),
     "lm_batch_stats_get": (_B, [_VP, _VP]),
     "lm_tune_entries": (_I, []),
+    "lm_serve_create": (_B, [_VP, ctypes.c_ulonglong]),
+    "lm_serve_submit": (_B, [_VP, _VP, _ULLP]),
+    "lm_serve_poll": (_I, [_VP, _VP, _I]),
+    "lm_serve_drain": (_B, [_VP, _LL]),
+    "lm_serve_stats_get": (_B, [_VP, _VP]),
+    "lm_serve_destroy": (None, [_VP]),
+    "lm_serve_replay": (_B, [_VP, _VP, _VP, _VP, _I, ctypes.c_uint, _VP]),
     "lm_launch_count": (ctypes.c_ulonglong, []),
     "lm_device_status": (ctypes.c_uint, [_VP]),
     "lm_prof_enable": (None, [_I]),
@@ -318,6 +325,108 @@ def job(buf, op, dims, elem_bytes=None):
     p, e = buf_ptr(buf, elem_bytes)
     d = list(dims) + [0] * (4 - len(dims))
     return Job(p, e, op, *d)
+
+
+class Request(ctypes.Structure):
+    """lm_request of include/lm_marshal.h."""
+    _fields_ = [("elem_bytes", ctypes.c_int), ("op", ctypes.c_int),
+                ("d0", ctypes.c_longlong), ("d1", ctypes.c_longlong),
+                ("d2", ctypes.c_longlong), ("d3", ctypes.c_longlong),
+                ("buf", ctypes.c_void_p), ("src", ctypes.c_void_p),
+                ("dst", ctypes.c_void_p)]
+
+
+class ServeDone(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_ulonglong), ("status", ctypes.c_int),
+                ("latency_ns", ctypes.c_longlong),
+                ("queue_ns", ctypes.c_longlong), ("done_ns", ctypes.c_longlong)]
+
+
+SERVE_PLAIN = 1
+
+
+def serve_replay(server, reqs, arrival_ns, after=None, plain=False):
+    """Replays a trace (list of Request, arrival offsets in ns, optional
+    dependency indices) through `server` (or alone per request with
+    plain=True); returns [(status, latency_ns, queue_ns)] per request."""
+    n = len(reqs)
+    arr = (Request * n)(*reqs)
+    t = (ctypes.c_longlong * n)(*[int(x) for x in arrival_ns])
+    a = (ctypes.c_int * n)(*([-1] * n if after is None else after))
+    out = (ServeDone * n)()
+    h = server.h if server is not None else None
+    _check(lib().lm_serve_replay(h, ctypes.cast(arr, ctypes.c_void_p),
+                                 ctypes.cast(t, ctypes.c_void_p),
+                                 ctypes.cast(a, ctypes.c_void_p), n,
+                                 SERVE_PLAIN if plain else 0,
+                                 ctypes.cast(out, ctypes.c_void_p)),
+           "lm_serve_replay")
+    return [(out[i].status, out[i].latency_ns, out[i].queue_ns)
+            for i in range(n)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_ulonglong) for n in (
+        "submitted", "completed", "batches", "bytes", "peak_inflight_bytes")]
+
+
+class Server:
+    """Owner of an lm_serve_t (a worker thread converting submitted
+    requests under an HBM budget, continuously batched)."""
+
+    def __init__(self, budget_bytes):
+        self.h = ctypes.c_void_p()
+        _check(lib().lm_serve_create(ctypes.byref(self.h), int(budget_bytes)),
+               "lm_serve_create")
+
+    def submit(self, op, dims, elem_bytes=None, buf=None, src=None, dst=None):
+        """In place on a device buffer (`buf`: CUDA tensor or pointer), or
+        host arrays `src` -> `dst` (pinned tensors or pointers) staged through
+        the server's pool.  Returns the ticket."""
+        d = list(dims) + [0] * (4 - len(dims))
+        r = Request()
+        if buf is not None:
+            p, e = buf_ptr(buf, elem_bytes)
+            r.buf = p
+        else:
+            e = int(elem_bytes or src.element_size())
+            r.src = src if isinstance(src, int) else src.data_ptr()
+            r.dst = dst if isinstance(dst, int) else dst.data_ptr()
+        r.elem_bytes, r.op = e, op
+        r.d0, r.d1, r.d2, r.d3 = d
+        t = ctypes.c_ulonglong(0)
+        _check(lib().lm_serve_submit(self.h, ctypes.byref(r), ctypes.byref(t)),
+               "lm_serve_submit")
+        return t.value
+
+    def poll(self, cap=4096):
+        """Completed requests: [(ticket, status, latency_ns, queue_ns)]."""
+        arr = (ServeDone * cap)()
+        n = lib().lm_serve_poll(self.h, ctypes.cast(arr, ctypes.c_void_p), cap)
+        if n < 0:
+            raise LMError("lm_serve_poll: bad arguments")
+        return [(arr[i].ticket, arr[i].status, arr[i].latency_ns,
+                 arr[i].queue_ns) for i in range(n)]
+
+    def drain(self, timeout_ms=-1):
+        _check(lib().lm_serve_drain(self.h, int(timeout_ms)), "lm_serve_drain")
+
+    def stats(self):
+        st = ServeStats()
+        _check(lib().lm_serve_stats_get(self.h, ctypes.byref(st)),
+               "lm_serve_stats_get")
+        return {n: getattr(st, n) for n, _ in ServeStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().lm_serve_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def finalize() -> None:
