@@ -488,6 +488,163 @@ def run_batch_workload(args, ws, rank, local):
 
 
 
+# ---- every measured configuration (plain per-op calls, CPU 1 and N threads) ---
+
+def run_configs_workload(args, ws, rank, local):
+    """GPU GB/s of the plain drop-in call for each configuration (inputs
+    resident, CUDA events, alternating directions so the buffer returns to
+    its layout), beside the reference's out-of-place CPU layout loop
+    (cpu_aos_asta / cpu_soa_asta restated in the oracle) on 1 and on all
+    host threads."""
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from libmarshal_gb300 import lm
+    from oracle import lm_oracle as O
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    L, OL = lm.lib(), O.lib()
+    nthreads = os.cpu_count() or 1
+    peak, peak_kind = peak_hbm()
+
+    def check(bad, what):
+        if bad:
+            raise RuntimeError(what + ": " + lm.last_error())
+
+    def gpu_rate(nbytes, steps, reps):
+        for k in range(3):
+            steps[k % len(steps)]()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        n = reps * len(steps)
+        e0.record(stream)
+        for k in range(n):
+            steps[k % len(steps)]()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        return ms, 2.0 * nbytes / (ms / 1e3) / 1e9
+
+    def cpu_rate(fn, nbytes, threads, budget_s):
+        fn(threads)  # warm the pages
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            fn(threads)
+            reps += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s:
+                break
+        return 2.0 * nbytes * reps / el / 1e9
+
+    rows = []
+
+    def case(name, e, nelem, steps, cpu_fn, cpu_bytes, reps=10, extra=None):
+        nbytes = nelem * e
+        ms, gbs = gpu_rate(nbytes, steps, reps)
+        row = {"config": name, "payload_bytes": nbytes, "gpu_ms": round(ms, 4),
+               "gpu_GBps": round(gbs, 1), "frac_of_peak": round(gbs / peak, 4)}
+        if cpu_fn is not None and not args.no_cpu:
+            row["cpu_1t_GBps"] = round(cpu_rate(cpu_fn, cpu_bytes, 1, 1.0), 2)
+            row["cpu_nt_GBps"] = round(cpu_rate(cpu_fn, cpu_bytes, nthreads,
+                                                1.0), 2)
+            row["cpu_threads"] = nthreads
+            row["cpu_sample_bytes"] = cpu_bytes
+        if extra:
+            row.update(extra)
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+
+    def dev_buf(nbytes, fill):
+        t = torch.empty((nbytes + 7) // 8, dtype=torch.int64, device=dev)
+        if fill == "random":
+            t.random_(generator=torch.Generator(device=dev).manual_seed(5))
+        return t
+
+    def host_pair(nelem, e):
+        src = np.empty(nelem * e, dtype=np.uint8)
+        OL.lmo_fill_splitmix64(src.ctypes.data, src.nbytes, 3)
+        return src, np.empty_like(src)
+
+    # cfg1: AoS [65536][7] fp32 -> ASTA t=32 and back (010(2048,32,7) and
+    # 010(2048,7,32)); 1.75 MiB stays in L2
+    h, w, t = 65536, 7, 32
+    b1 = dev_buf(h * w * 4, "random")
+    p1 = b1.data_ptr()
+    s1, d1 = host_pair(h * w, 4)
+    case("cfg1 AoS->ASTA fp32 [65536][7] t=32 (+ inverse)", 4, h * w,
+         [lambda: check(L.lm_aos_asta(sp, p1, 4, h, w, t, 1), "aos_asta"),
+          lambda: check(L.lm_transpose_010_bs(sp, p1, 4, h // t, w, t, None),
+                        "asta_aos")],
+         lambda th: OL.lmo_aos_asta_mt(s1.ctypes.data, d1.ctypes.data, h, w,
+                                       t, 4, th), h * w * 4, reps=200,
+         extra={"note": "1.75 MiB: L2-resident, launch-bound"})
+    del b1
+
+    # cfg2: 7200x1800 full transpose through the staged planner, 4 widths
+    M, N = 7200, 1800
+    A, a, B, b = 72, 100, 18, 100
+    st = O.alg3(A, a, B, b)
+    for e in (1, 2, 4, 8):
+        b2 = dev_buf(M * N * e, "random")
+        p2 = b2.data_ptr()
+        s2, d2 = host_pair(M * N, e)
+        case("cfg2 7200x1800 staged (a=100,b=100, stage %d) e=%d" % (st, e),
+             e, M * N,
+             [lambda: check(L.lm_transpose(sp, p2, e, A, a, B, b, 1, st, None),
+                            "transpose"),
+              lambda: check(L.lm_transpose(sp, p2, e, B, b, A, a, 1,
+                                           O.alg3(B, b, A, a), None),
+                            "transpose back")],
+             lambda th: OL.lmo_soa_asta_mt(s2.ctypes.data, d2.ctypes.data, N,
+                                           M, 1, e, th), M * N * e, reps=10)
+        del b2
+
+    # cfg3: fp32 16384x12289 plain 100, fp64 32768x16000, SoA->ASTA 2^27x4
+    for (AA, BB, e) in ((16384, 12289, 4), (32768, 16000, 8)):
+        b3 = dev_buf(AA * BB * e, "random")
+        p3 = b3.data_ptr()
+        # CPU sample: the first 2048 rows (same per-byte cost), to stay
+        # within seconds on one thread
+        rows_s = min(AA, 2048)
+        s3, d3 = host_pair(rows_s * BB, e)
+        case("cfg3 plain 100(%d,%d,1) e=%d" % (AA, BB, e), e, AA * BB,
+             [lambda: check(L.lm_transpose_100(sp, p3, e, AA, BB, 1, None),
+                            "100"),
+              lambda: check(L.lm_transpose_100(sp, p3, e, BB, AA, 1, None),
+                            "100 back")],
+             lambda th: OL.lmo_soa_asta_mt(s3.ctypes.data, d3.ctypes.data,
+                                           BB, rows_s, 1, e, th),
+             rows_s * BB * e, reps=5)
+        del b3
+        torch.cuda.empty_cache()
+    hh, ww, tt = 1 << 27, 4, 32
+    b4 = dev_buf(hh * ww * 4, "random")
+    p4 = b4.data_ptr()
+    sub = 1 << 22  # CPU sample: 2^22 records
+    s4, d4 = host_pair(sub * ww, 4)
+    for m, mname in ((0, "auto"), (2, "pttwac"), (5, "cycles")):
+        case("cfg3 SoA->ASTA %d x %d int32 t=%d = 100(4,2^22,32) [%s]"
+             % (hh, ww, tt, mname), 4, hh * ww,
+             [lambda: check(L.lm_transpose_0100_method(
+                 sp, p4, 4, 1, ww, hh // tt, tt, m, None), "soa_asta"),
+              lambda: check(L.lm_transpose_0100_method(
+                  sp, p4, 4, 1, hh // tt, ww, tt, m, None), "asta_soa")],
+             (lambda th: OL.lmo_soa_asta_mt(s4.ctypes.data, d4.ctypes.data,
+                                            sub, ww, tt, 4, th))
+             if m == 0 else None, sub * ww * 4, reps=5)
+    del b4
+    line = {"metric": "config_table_GBps", "value": rows[-1]["gpu_GBps"],
+            "unit": "GB/s", "n_gpus": ws, "steps": len(rows), "warmup": 3,
+            "higher_is_better": True, "peak": peak, "peak_kind": peak_kind,
+            "data": "synthetic (seeded random bits)", "rows": rows}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
 # ---- served workload (Poisson arrivals, continuous batching) -----------------
 
 SERVE_OPS = ("aos_asta", "asta_aos", "soa_asta", "asta_soa", "transpose")
@@ -622,7 +779,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU-baseline leg")
     ap.add_argument("--workload", default="headline",
-                    choices=["headline", "batch", "serve"])
+                    choices=["headline", "batch", "serve", "configs"])
     ap.add_argument("--batch-n", type=int, default=4096,
                     help="matrices in the batched workload")
     ap.add_argument("--skip-plain", action="store_true",
@@ -644,6 +801,8 @@ def main():
         return run_batch_workload(args, ws, rank, local)
     if args.workload == "serve":
         return run_serve_workload(args, ws, rank, local)
+    if args.workload == "configs":
+        return run_configs_workload(args, ws, rank, local)
     return run_ours(args, ws, rank, local)
 
 

@@ -99,7 +99,9 @@ bool lm_transpose_0100(lm_stream_t stream, void *buf, int elem_bytes, int A,
 /* 0100 with the algorithm forced: 0 = planner, 1 = BS (on-chip tiles),
  * 2 = PTTWAC on b-element units, 3 = stash (A == 1 only: save the half that
  * is overwritten first, then a streaming wavefront), 4 = two passes (BS on
- * tiles that make >= 128-byte units, then PTTWAC on those units).  Returns
+ * tiles that make >= 128-byte units, then PTTWAC on those units), 5 = whole
+ * cycles (when every cycle of 100(a, B) has at most 32 units: find each
+ * cycle's smallest position, then move whole cycles through registers).  Returns
  * true when the forced algorithm does not apply to the shape.  No reference
  * counterpart (the reference picks by super-element size,
  * cl_marshal.cc:365-370). */

@@ -203,7 +203,7 @@ static uint64_t wait_timeout_ns() {
 
 // ---- planner ----------------------------------------------------------------
 
-enum class Method { Auto, BS, Pttwac, Stash, TwoPass };
+enum class Method { Auto, BS, Pttwac, Stash, TwoPass, Cycles };
 
 static bool check_launch(cudaError_t e, const char *what) {
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -271,6 +271,23 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
                   (unsigned long long)(a * B * b * e));
   }
   const uint64_t U = b * e;
+  // all cycles short (multiplicative order of a modulo a*B - 1 at most
+  // kCycleMaxLen): whole-cycle moves, 2 x payload, no flags (lm_cycles.cu)
+  if (m == Method::Cycles ||
+      (m == Method::Auto && U >= 64 && !getenv("LM_NO_CYCLES"))) {
+    const uint32_t L = cycle_order(a, B, kCycleMaxLen);
+    if (L && a * B - 1 <= (1ull << 28)) {
+      Scratch sc;
+      if (get_scratch(sc, cycle_scratch_bytes(a, B), s)) return true;
+      return check_launch(launch_cycles100(s, buf, e, T, (uint32_t)a,
+                                           (uint32_t)B, (uint32_t)b, L, sc.p),
+                          "cycles launch");
+    }
+    if (m == Method::Cycles)
+      return fail("cycles: the cycles of 100(%llu, %llu) are longer than %u",
+                  (unsigned long long)a, (unsigned long long)B,
+                  (unsigned)kCycleMaxLen);
+  }
   const bool want_stash =
       m == Method::Stash ||
       (m == Method::Auto && T == 1 && U < 128 && a * B >= (1ull << 20) &&
@@ -377,6 +394,8 @@ static bool method_applies(Method m, int e, uint64_t T, uint64_t a,
       return b * e < 128 && (split_a(a, B, b, e) || split_B(a, B, b, e));
     case Method::BS:
       return plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e).feasible;
+    case Method::Cycles:
+      return cycle_order(a, B, kCycleMaxLen) != 0 && a * B - 1 <= (1ull << 28);
     default:
       return true;
   }
@@ -392,9 +411,10 @@ static Method tuned_method(cudaStream_t s, int e, uint64_t T, uint64_t a,
     if (it != g_tune.end()) return (Method)it->second;
   }
   const uint64_t bytes = T * a * B * b * (uint64_t)e;
-  Method cand[4];
+  Method cand[5];
   int nc = 0;
   cand[nc++] = Method::Auto;
+  if (method_applies(Method::Cycles, e, T, a, B, b)) cand[nc++] = Method::Cycles;
   if (T == 1 && plan_stash(a, B, (uint32_t)b, e).feasible) cand[nc++] = Method::Stash;
   if (b * e < 128 && (split_a(a, B, b, e) || split_B(a, B, b, e)))
     cand[nc++] = Method::TwoPass;
@@ -604,11 +624,12 @@ bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
                               unsigned long long *et) {
   OpTimer t(et, (cudaStream_t)stream);
   if (A < 0 || a < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
-  if (method < 0 || method > 4) return fail("method must be 0..4");
+  if (method < 0 || method > 5) return fail("method must be 0..5");
   const Method m = method == 1   ? Method::BS
                    : method == 2 ? Method::Pttwac
                    : method == 3 ? Method::Stash
                    : method == 4 ? Method::TwoPass
+                   : method == 5 ? Method::Cycles
                                  : Method::Auto;
   if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
               (uint64_t)B, (uint64_t)b, m))

@@ -1,0 +1,194 @@
+// lm_cycles.cu -- 100/0100 by whole-cycle moves, for shapes whose cycles are
+// all short.
+//
+// An in-place 100(A, B) on units moves the unit at position p to A*p mod M,
+// M = A*B - 1 (positions 0 and M stay): the same rule the reference's
+// cycle-following kernels walk one step at a time with a done flag per unit
+// (Transposition::Next, include/plan.hpp:54-56; _transpose_100,
+// src/cl/cl_aos_asta.cl:352-717).  When the multiplicative order L of A
+// modulo M is small (e.g. L = 12 for the SoA->ASTA shape 100(4, 2^22, 32),
+// where M = 2^24 - 1), every cycle has at most L units, so:
+//  * k_cycle_leaders finds each cycle's smallest position (walk at most L-1
+//    steps from every position; a warp appends its leaders with one atomic);
+//  * k_cycle_move gives each (cycle, granule of a unit, tile) to one thread,
+//    which loads the granule of all L units into registers, then stores each
+//    one a step further along the cycle.
+// No flags, no waits; every unit is read once and written once, in granules
+// of up to 16 bytes (8 for cycles longer than 16 units, to stay in
+// registers), so a unit of >= 32 bytes moves as whole sectors.
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <algorithm>
+
+#include "lm_core.cuh"
+#include "lm_internal.h"
+
+namespace lm {
+
+namespace {
+
+constexpr int kCycThreads = 256;
+
+// x * y mod M for x, y < M < 2^32 by Barrett reduction with
+// minv = floor((2^64 - 1) / M): the estimate is off by at most one M.
+struct ModM {
+  uint64_t M;
+  uint64_t minv;
+};
+
+__device__ __forceinline__ uint32_t mulmod(uint64_t x, uint64_t y,
+                                           const ModM &m) {
+  const uint64_t p = x * y;
+  const uint64_t q = __umul64hi(p, m.minv);
+  uint64_t r = p - q * m.M;
+  if (r >= m.M) r -= m.M;
+  return (uint32_t)r;
+}
+
+__global__ void __launch_bounds__(kCycThreads)
+    k_cycle_leaders(uint32_t A, ModM m, uint32_t L, uint32_t *list,
+                    uint32_t *count) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // every warp runs the same number of iterations (ballot below)
+  const uint64_t n = m.M - 1;  // positions 1 .. M-1
+  const uint64_t iters = (n + stride - 1) / stride;
+  uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
+  for (uint64_t it = 0; it < iters; ++it, p += stride) {
+    bool lead = false;
+    if (p < m.M) {
+      uint32_t q = mulmod(A, p, m);
+      lead = q != p;  // fixed points move nothing
+      for (uint32_t k = 1; lead && q != p && k < L; ++k) {
+        if (q < p) lead = false;
+        q = mulmod(A, q, m);
+      }
+    }
+    const unsigned mask = __ballot_sync(kFull, lead);
+    if (mask) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(count, (uint32_t)__popc(mask));
+      base = __shfl_sync(kFull, base, 0);
+      if (lead) list[base + __popc(mask & ((1u << lane) - 1))] = (uint32_t)p;
+    }
+  }
+}
+
+template <int G, int LMAX>
+__global__ void __launch_bounds__(kCycThreads, 2)
+    k_cycle_move(char *base, uint64_t T, uint64_t tile_bytes, uint32_t U,
+                 uint32_t A, ModM m, const uint32_t *list,
+                 const uint32_t *count) {
+  using V = typename Vec<G>::T;
+  const uint32_t gpu = U / G;  // granules per unit
+  const uint64_t ncyc = *count;
+  const uint64_t total = ncyc * gpu * T;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+       idx < total; idx += (uint64_t)gridDim.x * blockDim.x) {
+    // granule fastest, then cycle, then tile
+    const uint64_t rest = idx / gpu;
+    const uint32_t g = (uint32_t)(idx - rest * gpu);
+    const uint64_t t = rest / ncyc;
+    const uint32_t c = (uint32_t)(rest - t * ncyc);
+    char *tb = base + t * tile_bytes + (uint64_t)g * G;
+    uint32_t pos[LMAX];
+    pos[0] = list[c];
+    int len = 1;
+#pragma unroll
+    for (int k = 1; k < LMAX; ++k) {
+      const uint32_t q = mulmod(A, pos[k - 1], m);
+      pos[k] = q;
+      if (len == k && q != pos[0]) len = k + 1;
+    }
+    V v[LMAX];
+#pragma unroll
+    for (int k = 0; k < LMAX; ++k)
+      if (k < len)
+        v[k] = __ldcs(reinterpret_cast<const V *>(tb + (uint64_t)pos[k] * U));
+#pragma unroll
+    for (int k = 0; k < LMAX; ++k)
+      if (k < len) {
+        const uint32_t d = k + 1 < len ? pos[(k + 1) % LMAX] : pos[0];
+        __stcs(reinterpret_cast<V *>(tb + (uint64_t)d * U), v[k]);
+      }
+  }
+}
+
+template <int G>
+cudaError_t launch_move(cudaStream_t s, char *base, uint64_t T,
+                        uint64_t tile_bytes, uint32_t U, uint32_t A,
+                        const ModM &m, uint32_t L, const uint32_t *list,
+                        const uint32_t *count) {
+  const DeviceInfo &di = device_info();
+  const unsigned grid = (unsigned)di.sms * 8;
+  ProfScope ps(s, "cycle_move");
+  if (L <= 8)
+    k_cycle_move<G, 8><<<grid, kCycThreads, 0, s>>>(base, T, tile_bytes, U, A,
+                                                     m, list, count);
+  else if (L <= 16)
+    k_cycle_move<G, 16><<<grid, kCycThreads, 0, s>>>(base, T, tile_bytes, U,
+                                                      A, m, list, count);
+  else
+    k_cycle_move<(G > 8 ? 8 : G), 32><<<grid, kCycThreads, 0, s>>>(
+        base, T, tile_bytes, U, A, m, list, count);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+uint32_t cycle_order(uint64_t A, uint64_t B, uint32_t limit) {
+  if (A < 2 || B < 2) return 0;
+  const unsigned __int128 M = (unsigned __int128)A * B - 1;
+  if (M >= ((unsigned __int128)1 << 32)) return 0;
+  const uint64_t m = (uint64_t)M;
+  uint64_t x = A % m;
+  for (uint32_t k = 1; k <= limit; ++k) {
+    if (x == 1) return k;
+    x = (uint64_t)(((unsigned __int128)x * A) % m);
+  }
+  return 0;
+}
+
+size_t cycle_scratch_bytes(uint64_t A, uint64_t B) {
+  const uint64_t M = A * B - 1;
+  // count word (padded) + a list with room for every nontrivial cycle
+  return 256 + ((M - 1) / 2 + 1) * sizeof(uint32_t);
+}
+
+cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
+                             uint32_t a, uint32_t B, uint32_t b, uint32_t L,
+                             void *scratch) {
+  const uint64_t M = (uint64_t)a * B - 1;
+  if (L == 0 || L > kCycleMaxLen || M >= (1ull << 32)) return cudaErrorInvalidValue;
+  ModM m;
+  m.M = M;
+  m.minv = ~0ull / M;
+  uint32_t *count = reinterpret_cast<uint32_t *>(scratch);
+  uint32_t *list = reinterpret_cast<uint32_t *>((char *)scratch + 256);
+  cudaError_t err = cudaMemsetAsync(count, 0, sizeof(uint32_t), s);
+  if (err != cudaSuccess) return err;
+  const DeviceInfo &di = device_info();
+  {
+    const uint64_t want = (M + kCycThreads - 1) / kCycThreads;
+    const unsigned grid =
+        (unsigned)std::min<uint64_t>(want, (uint64_t)di.sms * 16);
+    ProfScope ps(s, "cycle_leaders");
+    k_cycle_leaders<<<grid, kCycThreads, 0, s>>>(a, m, L, list, count);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  const uint32_t U = b * (uint32_t)e;
+  const uint64_t tile_bytes = (uint64_t)a * B * U;
+  const uintptr_t addr = (uintptr_t)buf;
+  auto fits = [&](uint32_t G) {
+    return U % G == 0 && addr % G == 0 && (T == 1 || tile_bytes % G == 0);
+  };
+  char *base = reinterpret_cast<char *>(buf);
+  if (fits(16)) return launch_move<16>(s, base, T, tile_bytes, U, a, m, L, list, count);
+  if (fits(8)) return launch_move<8>(s, base, T, tile_bytes, U, a, m, L, list, count);
+  if (fits(4)) return launch_move<4>(s, base, T, tile_bytes, U, a, m, L, list, count);
+  if (fits(2)) return launch_move<2>(s, base, T, tile_bytes, U, a, m, L, list, count);
+  return launch_move<1>(s, base, T, tile_bytes, U, a, m, L, list, count);
+}
+
+}  // namespace lm

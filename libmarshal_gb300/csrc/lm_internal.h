@@ -100,6 +100,19 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
 
 // The per-op planner (lm_api.cu) for one 0100; tune != 0 lets the
 // autotuner pick the algorithm of this shape class.
+// ---- whole-cycle moves (lm_cycles.cu) ----------------------------------------
+// Cycles held in registers: at most this many units.
+constexpr uint32_t kCycleMaxLen = 32;
+// Multiplicative order of a modulo a*B - 1 (the length every cycle of a
+// 100(a, B) divides), or 0 when it exceeds `limit` or a*B - 1 >= 2^32.
+uint32_t cycle_order(uint64_t a, uint64_t B, uint32_t limit);
+size_t cycle_scratch_bytes(uint64_t a, uint64_t B);
+// T instances of 100(a, B, b) whose cycles have at most L <= kCycleMaxLen
+// units; `scratch` holds cycle_scratch_bytes(a, B) bytes.
+cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
+                             uint32_t a, uint32_t B, uint32_t b, uint32_t L,
+                             void *scratch);
+
 // An LM_OP_* with its dimensions as the 0100(T, a, B, b) it performs; false
 // for an unknown op or bad dimensions (lm_batch.cu).
 bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
