@@ -277,8 +277,14 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
       (m == Method::Auto && U >= 64 && !getenv("LM_NO_CYCLES"))) {
     const uint32_t L = cycle_order(a, B, kCycleMaxLen);
     if (L && a * B - 1 <= (1ull << 28)) {
+      // leader lists are cached per shape, except under stream capture
+      // (where the list is computed into per-call scratch)
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      cudaStreamIsCapturing(s, &cs);
       Scratch sc;
-      if (get_scratch(sc, cycle_scratch_bytes(a, B), s)) return true;
+      if (cs != cudaStreamCaptureStatusNone &&
+          get_scratch(sc, cycle_scratch_bytes(a, B), s))
+        return true;
       return check_launch(launch_cycles100(s, buf, e, T, (uint32_t)a,
                                            (uint32_t)B, (uint32_t)b, L, sc.p),
                           "cycles launch");
@@ -570,6 +576,7 @@ const char *lm_version(void) { return "libmarshal_gb300 1.0 (sm_103a)"; }
 void lm_marshal_finalize(void) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return;
+  cycle_cache_clear();
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
     cudaMemPoolTrimTo(pool, 0);

@@ -107,8 +107,13 @@ constexpr uint32_t kCycleMaxLen = 32;
 // 100(a, B) divides), or 0 when it exceeds `limit` or a*B - 1 >= 2^32.
 uint32_t cycle_order(uint64_t a, uint64_t B, uint32_t limit);
 size_t cycle_scratch_bytes(uint64_t a, uint64_t B);
+// Frees the cached cycle-leader lists of the current device (waits for
+// their readers).
+void cycle_cache_clear();
 // T instances of 100(a, B, b) whose cycles have at most L <= kCycleMaxLen
-// units; `scratch` holds cycle_scratch_bytes(a, B) bytes.
+// units.  With `scratch` (cycle_scratch_bytes(a, B) bytes) the cycle leaders
+// are computed there; with nullptr they come from a per-device cache of
+// recent shapes (not to be used while the stream is being captured).
 cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
                              uint32_t a, uint32_t B, uint32_t b, uint32_t L,
                              void *scratch);

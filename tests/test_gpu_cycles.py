@@ -72,3 +72,27 @@ def test_planner_picks_cycles_for_soa_asta(cuda):
     assert "cycle_move" in kernels, kernels
     got = buf.cpu().numpy().view(np.uint32)
     assert np.array_equal(got, O.soa_asta(src, h, w, t))
+
+
+def test_cycles_cached_leaders_across_streams(cuda):
+    """The leader list of a shape is computed once and reused from another
+    stream (which waits for it); finalize drops it and it is rebuilt."""
+    import torch
+    from libmarshal_gb300 import lm
+    T, a, B, b, e = 1, 4, 1 << 14, 32, 4
+    n = a * B * b
+    srcs = [O.random_bits(n, e, 600 + k) for k in range(3)]
+    want = [O.t0100(s, T, a, B, b) for s in srcs]
+    bufs = [torch.from_numpy(s.view(np.uint8).copy()).to(cuda) for s in srcs]
+    streams = [torch.cuda.Stream() for _ in range(2)]
+    torch.cuda.synchronize()
+    for k, buf in enumerate(bufs):
+        if k == 2:
+            lm.finalize()
+        st = streams[k % 2]
+        assert not lm.lib().lm_transpose_0100_method(
+            st.cuda_stream, buf.data_ptr(), e, T, a, B, b, 5, None), \
+            lm.last_error()
+    torch.cuda.synchronize()
+    for buf, w in zip(bufs, want):
+        assert np.array_equal(buf.cpu().numpy().view(O.DTYPES[e]), w)
