@@ -85,6 +85,7 @@ struct StashPlan {
   uint32_t pitch = 0;          // shared bytes per gathered row
   size_t smem_bytes = 0;
   int ctas_per_sm = 1;
+  uint32_t margin = 0;         // steps of slack between CTAs
   size_t stash_bytes = 0;
 };
 StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e);
@@ -98,8 +99,6 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
                             void *scratch, uint32_t *status,
                             uint64_t timeout_ns);
 
-// The per-op planner (lm_api.cu) for one 0100; tune != 0 lets the
-// autotuner pick the algorithm of this shape class.
 // ---- whole-cycle moves (lm_cycles.cu) ----------------------------------------
 // Cycles held in registers: at most this many units.
 constexpr uint32_t kCycleMaxLen = 32;
@@ -123,6 +122,8 @@ cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
 bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
                 uint64_t *T, uint64_t *a, uint64_t *B, uint64_t *b);
 
+// The per-op planner (lm_api.cu) for one 0100; tune != 0 lets the
+// autotuner pick the algorithm of this shape class.
 bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
                       uint64_t a, uint64_t B, uint64_t b, int tune);
 

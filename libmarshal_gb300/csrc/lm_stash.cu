@@ -463,10 +463,13 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
 // --- host side ---------------------------------------------------------------
 
 // Row pitch of a gathered strip: room for the 16-byte aligned superset a
-// bulk copy fetches, and an odd number of 16-byte words.
+// bulk copy fetches (at most round16(len) + 16 bytes), and an odd number of
+// 16-byte words so that 8 consecutive rows start in distinct bank groups.
 static uint32_t stash_pitch(uint64_t row_bytes, int e) {
   (void)e;
-  return (uint32_t)((row_bytes + 15) / 16 * 16 + 32);
+  uint64_t p = (row_bytes + 15) / 16 * 16 + 16;
+  if (((p / 16) & 1) == 0) p += 16;
+  return (uint32_t)p;
 }
 
 template <int E>
@@ -506,6 +509,9 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
   uint64_t strips[3] = {strips_default[0], strips_default[1], strips_default[2]};
   if (es && atoll(es) > 0) strips[0] = strips[1] = strips[2] = (uint64_t)atoll(es);
   const int per_sms[2] = {ep && atoi(ep) == 1 ? 1 : 2, 1};
+  const char *em = getenv("LM_STASH_MARGIN");
+  const uint32_t margin =
+      em && atoi(em) > 0 && atoi(em) < 64 ? (uint32_t)atoi(em) : kStashMargin;
   for (uint64_t strip : strips) {
     uint64_t g = std::max<uint64_t>(1, strip / U);
     if (g > B) g = B;
@@ -513,7 +519,12 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
     const uint32_t pitch = stash_pitch(g * U, e);
     for (int per_sm : per_sms) {
       const uint64_t ctas = (uint64_t)di.sms * per_sm;
-      const uint64_t W = (A + ctas - 1) / ctas;
+      // rows per chunk a multiple of 8 (when that still leaves >= 3/4 of
+      // the CTAs busy), so each chunk's output segments start on 32-byte
+      // sectors and the writers' 8-row patches stay whole
+      uint64_t W = (A + ctas - 1) / ctas;
+      const uint64_t W8 = (W + 7) / 8 * 8;
+      if ((A + W8 - 1) / W8 * 4 >= ctas * 3) W = W8;
       const uint64_t smem = (uint64_t)kStages * stash_stage_bytes(W, pitch);
       if (smem > max_smem / per_sm) continue;
       if (W * g * b >= 0xffffffffull || g * b >= 0xffffffffull) continue;
@@ -530,9 +541,10 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
       p.pitch = pitch;
       p.smem_bytes = (size_t)smem;
       p.ctas_per_sm = per_sm;
+      p.margin = margin;
       uint64_t total = 0;
       for (uint64_t J = 0; J < G; ++J)
-        total += stash_rows(J, g, A, B, kStashMargin);
+        total += stash_rows(J, g, A, B, margin);
       p.stash_bytes = (size_t)(total * g * U);
       return p;
     }
@@ -662,7 +674,7 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   g.timeout_ns = timeout_ns;
   g.trace = nullptr;
   g.trace_ctas = 0;
-  g.margin = kStashMargin;
+  g.margin = p.margin;
   {
     const char *gm = getenv("LM_STASH_GATHER");
     g.tma = (gm && gm[0] == 'c') ? 0u : 1u;  // "cpasync" selects cp.async
