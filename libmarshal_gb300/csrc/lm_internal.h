@@ -86,6 +86,7 @@ struct StashPlan {
   size_t smem_bytes = 0;
   int ctas_per_sm = 1;
   uint32_t margin = 0;         // steps of slack between CTAs
+  uint64_t A = 0;              // rows (the row-offset table has A+1 words)
   size_t stash_bytes = 0;
 };
 StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e);

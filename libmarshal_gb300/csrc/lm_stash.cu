@@ -16,8 +16,11 @@
 //   must be saved: for group J these are exactly the rows i < r(J) =
 //   ceil(g*J*(A-1)/B) (half of the matrix over all J).
 //
-//   K1 (k_stash_save): copies rows i < r(J) of every column group J into a
-//   compact stash (stream-ordered scratch): reads and writes half the data.
+//   Row i is read from the stash by every group J >= J_i (the first group
+//   with i < r(J)), so the stash holds one contiguous suffix per row: units
+//   [J_i*g, B) of row i, at the same address modulo 16 as in the buffer.
+//   K0 (k_stash_offsets) lays the suffixes out; K1 (k_stash_save) copies
+//   them with 16-byte vectors (a memcpy of half the data).
 //   K2 (k_stash_wave): a persistent grid; CTA c owns the source rows
 //   [c*W, (c+1)*W).  For each J it gathers its rows' group-J strip (from the
 //   stash for i < r(J), from the buffer otherwise) into shared memory,
@@ -38,11 +41,12 @@ namespace lm {
 struct StashArgs {
   char *base;
   char *stash;
-  const uint64_t *soff;  // byte offset of each group's stash block, G+1
+  const uint64_t *roff;  // byte offset of each row's stash suffix, A+1
   uint32_t *progress;    // one counter per row chunk
   uint32_t *status;
   uint64_t A, B;         // rows, columns (units)
   uint32_t b;            // elements per unit
+  uint32_t e;            // bytes per element
   uint32_t g;            // units per column group
   uint32_t G;            // groups
   uint32_t W;            // rows per chunk
@@ -56,7 +60,17 @@ struct StashArgs {
   uint32_t tma;          // 1: gather rows with bulk copies, 0: cp.async
   uint64_t *trace;       // debug: per (chunk, step) timestamps, or null
   uint32_t trace_ctas;
+  // first stashed group of a row (stash_first_group) without a division:
+  // i*B and g*(A-1) are < 2^32
+  uint64_t gAk;          // g*A*margin
+  FastDiv div_D;         // g*(A-1)
+  FastDiv div_Bc, div_Wc;  // B and W (chunk of a position)
 };
+
+__device__ __forceinline__ uint64_t first_group(uint64_t i, const StashArgs &g) {
+  const uint64_t lhs = i * g.B;
+  return lhs < g.gAk ? 0 : (uint64_t)fdiv((uint32_t)(lhs - g.gAk), g.div_D) + 1;
+}
 
 // Bytes of one ring stage: W rows of `pitch` bytes, then W uint32 row
 // offsets; rounded to 128 so every stage (a bulk-copy destination) stays
@@ -80,97 +94,126 @@ __host__ __device__ __forceinline__ uint64_t stash_rows(uint64_t J, uint64_t g,
   return r < A ? r : A;
 }
 
-// K0: stash offsets: per-thread partial sums over a range of groups, then a
-// block-wide exclusive scan of the 1024 partials (warp shuffles).
-__global__ void k_stash_offsets(uint64_t *soff, uint64_t A, uint64_t B,
-                                uint32_t g, uint32_t G, uint64_t row_bytes,
-                                uint64_t k) {
+// First group J_i that reads row i from the stash: the smallest J with
+// i < r(J), i.e. g*(A-1)*J > i*B - g*A*k.  J_i >= G: row i is not stashed.
+__host__ __device__ __forceinline__ uint64_t stash_first_group(
+    uint64_t i, uint64_t g, uint64_t A, uint64_t B, uint64_t k) {
+  const uint64_t lhs = i * B, rhs = g * A * k;
+  return lhs < rhs ? 0 : (lhs - rhs) / (g * (A - 1)) + 1;
+}
+
+// Bytes of row i's stash slot: the suffix rounded up to 16 bytes, plus 16
+// so the data can start at its buffer address modulo 16.
+__host__ __device__ __forceinline__ uint64_t stash_slot_bytes(
+    uint64_t i, uint64_t g, uint64_t A, uint64_t B, uint64_t G, uint64_t U,
+    uint64_t k) {
+  const uint64_t Ji = stash_first_group(i, g, A, B, k);
+  if (Ji >= G) return 0;
+  return ((B - Ji * g) * U + 15) / 16 * 16 + 16;
+}
+
+// K0: per-row stash offsets, one block of 32 warps: warp w owns a contiguous
+// range of rows and walks it 32 rows at a time (lane l: row base + l, so
+// the table writes are coalesced), with warp-shuffle scans; a first pass
+// sums each warp's range, the 32 sums are scanned, a second pass writes
+// roff[i] = slot start + (buffer address of the row's suffix mod 16).
+__global__ void __launch_bounds__(1024) k_stash_offsets(StashArgs sa) {
   __shared__ uint64_t warp_tot[32];
-  const uint32_t t = threadIdx.x, nt = blockDim.x;
-  const uint32_t lane = t & 31, warp = t >> 5;
-  const uint32_t per = (G + nt - 1) / nt;
-  const uint32_t j0 = min(G, t * per), j1 = min(G, j0 + per);
-  uint64_t part = 0;
-  for (uint32_t J = j0; J < j1; ++J) part += stash_rows(J, g, A, B, k) * row_bytes;
-  // inclusive scan within the warp
-  uint64_t inc = part;
+  uint64_t *roff = const_cast<uint64_t *>(sa.roff);
+  const uint64_t A = sa.A, B = sa.B, g = sa.g, G = sa.G;
+  const uint64_t U = (uint64_t)sa.b * sa.e;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t per = (A + 31) / 32;
+  const uint64_t r0 = min64(A, (uint64_t)warp * per), r1 = min64(A, r0 + per);
+  auto slot = [&](uint64_t Ji) -> uint64_t {
+    return Ji >= G ? 0 : ((B - Ji * g) * U + 15) / 16 * 16 + 16;
+  };
+  uint64_t sum = 0;  // lane-private partial of this warp's range
+  for (uint64_t i = r0 + lane; i < r1; i += 32) sum += slot(first_group(i, sa));
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint64_t v = __shfl_up_sync(kFull, inc, o);
-    if (lane >= (uint32_t)o) inc += v;
-  }
-  if (lane == 31) warp_tot[warp] = inc;
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+  if (lane == 0) warp_tot[warp] = sum;
   __syncthreads();
   if (warp == 0) {
-    const uint32_t nw = nt / 32;
-    uint64_t w = lane < nw ? warp_tot[lane] : 0;
+    uint64_t w = warp_tot[lane];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint64_t v = __shfl_up_sync(kFull, w, o);
       if (lane >= (uint32_t)o) w += v;
     }
-    if (lane < nw) warp_tot[lane] = w;  // inclusive over warps
+    warp_tot[lane] = w;  // inclusive over warps
   }
   __syncthreads();
-  uint64_t acc = inc - part + (warp ? warp_tot[warp - 1] : 0);
-  for (uint32_t J = j0; J < j1; ++J) {
-    soff[J] = acc;
-    acc += stash_rows(J, g, A, B, k) * row_bytes;
+  uint64_t carry = warp ? warp_tot[warp - 1] : 0;
+  for (uint64_t base_i = r0; base_i < r1; base_i += 32) {
+    const uint64_t i = base_i + lane;
+    uint64_t Ji = 0, sz = 0;
+    if (i < r1) {
+      Ji = first_group(i, sa);
+      sz = slot(Ji);
+    }
+    uint64_t inc = sz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t v = __shfl_up_sync(kFull, inc, o);
+      if (lane >= (uint32_t)o) inc += v;
+    }
+    if (i < r1) {
+      const uintptr_t src = (uintptr_t)sa.base + (i * B + Ji * g) * U;
+      roff[i] = carry + inc - sz + (src & 15);
+    }
+    carry += __shfl_sync(kFull, inc, 31);
   }
-  if (t == nt - 1) soff[G] = acc;
+  if (threadIdx.x == 1023) roff[A] = warp_tot[31];
 }
 
-// K1: copy the rows that are overwritten before they are consumed.
-// grid.x: row blocks of kSaveRows rows, grid.y: column groups.
-constexpr uint32_t kSaveRows = 32;
+// K1: copy every row's stash suffix: one warp per row at a time, 16-byte
+// vectors between the (equally misaligned) buffer and stash addresses, the
+// ragged head and tail bytes one by one.
 constexpr int kSaveThreads = 256;
 
-template <int E>
 __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
-  using T = typename Elem<E>::T;
-  const uint32_t J = blockIdx.y;
-  const uint64_t r = stash_rows(J, g.g, g.A, g.B, g.margin);
-  const uint64_t i0 = (uint64_t)blockIdx.x * kSaveRows;
-  if (i0 >= r) return;
-  const uint32_t nrows = (uint32_t)min64(kSaveRows, r - i0);
-  const uint64_t col0 = (uint64_t)J * g.g;
-  const uint32_t gj = (uint32_t)min64(g.g, g.B - col0);
-  const uint32_t n_row = gj * g.b;  // elements per row strip
-  const uint32_t n = nrows * g.gb;
-  const T *src = reinterpret_cast<const T *>(g.base);
-  T *dst = reinterpret_cast<T *>(g.stash + g.soff[J]) + i0 * g.gb;
-  for (uint32_t t = threadIdx.x; t < n; t += kSaveThreads * 4) {
-    T v[4];
-    uint32_t k[4];
-    uint64_t row[4];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = ((uint64_t)blockIdx.x * kSaveThreads + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * kSaveThreads) >> 5;
+  const uint64_t U = (uint64_t)g.b * g.e;
+  for (uint64_t i = gw; i < g.A; i += nw) {
+    const uint64_t Ji = first_group(i, g);
+    if (Ji >= g.G) continue;
+    const char *src = g.base + (i * g.B + Ji * g.g) * U;
+    char *dst = g.stash + g.roff[i];
+    const uint64_t n = (g.B - Ji * g.g) * U;
+    const uint64_t head = min64((16 - ((uintptr_t)src & 15)) & 15, n);
+    const uint64_t nvec = (n - head) / 16;
+    const uint64_t tail0 = head + nvec * 16;
+    if (lane < head) dst[lane] = src[lane];
+    if (lane < n - tail0) dst[tail0 + lane] = src[tail0 + lane];
+    const uint4 *vs = reinterpret_cast<const uint4 *>(src + head);
+    uint4 *vd = reinterpret_cast<uint4 *>(dst + head);
+    for (uint64_t v = lane; v < nvec; v += 32 * 4) {
+      uint4 x[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t tt = t + u * kSaveThreads;
-      const uint32_t rr = fdiv(tt, g.div_gb);
-      k[u] = tt - rr * g.gb;
-      row[u] = i0 + rr;
-      if (tt < n && k[u] < n_row)
-        v[u] = __ldcg(src + (row[u] * g.B + col0) * g.b + k[u]);
-    }
+      for (int u = 0; u < 4; ++u)
+        if (v + 32 * u < nvec) x[u] = __ldcs(vs + v + 32 * u);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t tt = t + u * kSaveThreads;
-      if (tt < n && k[u] < n_row) __stcg(dst + tt, v[u]);
+      for (int u = 0; u < 4; ++u)
+        if (v + 32 * u < nvec) __stcg(vd + v + 32 * u, x[u]);
     }
   }
 }
 
 // K2: the wavefront, warp-specialised.  Per CTA:
-//   warps 0-3 (producers): gather step J into ring stage J % kStages with
-//     16-byte cp.async copies of a 16-byte aligned superset of every row
-//     strip (rowoff[] records where the strip starts); completion arrives on
-//     the stage's `full` barrier;
-//   warp 4 (poller): when stage J has landed, publishes progress = J+1, then
-//     waits for the CTAs whose rows hold original data in its destination
-//     range and releases the stage to the writers;
-//   warps 5.. (writers): write step J from the stage, then free it.
-// Stages are handed over with mbarriers (full / ready / empty); every wait is
-// bounded by %globaltimer; a timeout sets the status word and all roles stop.
+//   warps 0-3 (producers): gather step J into ring stage J % kStages (warp 0
+//     issues one bulk copy per row of a 16-byte aligned superset of its
+//     strip, rowoff[] records where the strip starts; or, with cp.async, all
+//     four warps copy 16-byte pieces); completion lands on `full`;
+//   warp 4 (publisher): when stage J has landed, publishes progress = J+1;
+//   warp 5 (checker): waits for the CTAs whose rows hold original data in
+//     step J's destination range, then marks the stage `ready`;
+//   warps 6.. (writers): write step J from the stage, then free it (`empty`,
+//     which the publisher also arrives on).
+// Every wait is bounded by %globaltimer; a timeout sets the status word and
+// all roles stop.
 constexpr int kWaveThreads = 512;
 constexpr int kStages = 3;
 constexpr int kProducerWarps = 4;
@@ -182,6 +225,9 @@ constexpr int kMaxRowBlocks = 4;  // rows per chunk <= 128
 constexpr uint32_t kStashMargin = 3;
 constexpr uint32_t kMaxChunks = 1024;  // CTAs of the wave (co-resident)
 constexpr uint32_t kProgStride = 32;   // one 128-byte line per progress word
+// LM_STASH_TRACE slots per (chunk, step): 0 gather issued, 1 published,
+// 2 stage ready (deps and ring), 3 written, 4 deps satisfied, 5 check begun
+constexpr int kTraceSlots = 8;
 
 template <int E>
 __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
@@ -209,7 +255,11 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], g.tma ? 1u : kProducerWarps * 32u);
       mbar_init(&ready[s], 1);
-      mbar_init(&empty[s], kWriterWarps);
+      // freed by every writer warp and by the publisher, so a stage is not
+      // refilled (its `full` barrier not completed again) before the
+      // publisher has seen the step in it: a parity wait that fell a whole
+      // ring behind would otherwise wait for the wrong phase
+      mbar_init(&empty[s], kWriterWarps + 1);
     }
     fence_mbar_init();
     s_ok = 1;
@@ -237,6 +287,14 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     const uint32_t pt = threadIdx.x;  // 0 .. 127
     constexpr uint32_t kP = kProducerWarps * 32;
     uint32_t issued = 0;
+    // this lane's rows t = lane + 32m: first stashed group and stash offset
+    uint64_t rJi[kMaxRowBlocks], rro[kMaxRowBlocks];
+#pragma unroll
+    for (int m = 0; m < kMaxRowBlocks; ++m) {
+      const uint32_t t = lane + 32 * m;
+      rJi[m] = t < Wc ? first_group(i0 + t, g) : ~0ull;
+      rro[m] = t < Wc ? g.roff[i0 + t] : 0;
+    }
     for (uint32_t J = 0; J < g.G; ++J) {
       const uint32_t s = J % kStages;
       bool stop = !s_ok;
@@ -255,17 +313,21 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
       issued = J + 1;
       const uint64_t col0 = (uint64_t)J * g.g;
       const uint32_t len = (uint32_t)min64(g.g, g.B - col0) * U;
-      const uint64_t r = stash_rows(J, g.g, g.A, g.B, g.margin);
-      const char *st = g.stash + g.soff[J];
       unsigned char *sb = stage(s);
+      // row i's strip: from its stash suffix when J >= J_i
+      auto strip = [&](uint64_t i, uint64_t Ji, uint64_t ro) -> const char * {
+        return J >= Ji ? g.stash + ro + (col0 - Ji * g.g) * U
+                       : g.base + (i * g.B + col0) * U;
+      };
       if (g.tma) {
         // warp 0: one bulk copy per row (16-byte aligned superset)
         if (warp == 0) {
           uint32_t bytes = 0;
-          for (uint32_t t = lane; t < Wc; t += 32) {
-            const uint64_t i = i0 + t;
-            const char *src = (i < r) ? st + i * g.g * U
-                                      : g.base + (i * g.B + col0) * U;
+#pragma unroll
+          for (int m = 0; m < kMaxRowBlocks; ++m) {
+            const uint32_t t = lane + 32 * m;
+            if (t >= Wc) continue;
+            const char *src = strip(i0 + t, rJi[m], rro[m]);
             const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
             const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
             bytes += (uint32_t)(a1 - a0);
@@ -277,13 +339,14 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
           fence_proxy_async_smem();
           __syncwarp();
           if (g.trace && ch < g.trace_ctas && lane == 0)
-            g.trace[((uint64_t)ch * g.G + J) * 4 + 0] = global_timer_ns();
+            g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 0] = global_timer_ns();
           if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
           __syncwarp();
-          for (uint32_t t = lane; t < Wc; t += 32) {
-            const uint64_t i = i0 + t;
-            const char *src = (i < r) ? st + i * g.g * U
-                                      : g.base + (i * g.B + col0) * U;
+#pragma unroll
+          for (int m = 0; m < kMaxRowBlocks; ++m) {
+            const uint32_t t = lane + 32 * m;
+            if (t >= Wc) continue;
+            const char *src = strip(i0 + t, rJi[m], rro[m]);
             const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
             const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
             bulk_g2s(sb + (size_t)t * g.pitch, (const void *)a0,
@@ -296,8 +359,7 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
         for (uint32_t w = pt; w < Wc * nc; w += kP) {
           const uint32_t t = w / nc, c = w - t * nc;
           const uint64_t i = i0 + t;
-          const char *src = (i < r) ? st + i * g.g * U
-                                    : g.base + (i * g.B + col0) * U;
+          const char *src = strip(i, first_group(i, g), g.roff[i]);
           const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
           const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
           if (c == 0)
@@ -307,7 +369,7 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
                        (const void *)(a0 + 16 * (uintptr_t)c));
         }
         if (g.trace && ch < g.trace_ctas && pt == 0)
-          g.trace[((uint64_t)ch * g.G + J) * 4 + 0] = global_timer_ns();
+          g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 0] = global_timer_ns();
         cp_async_mbar_arrive_noinc(&full[s]);
       }
     }
@@ -333,7 +395,8 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
       if (!__all_sync(kFull, landed)) break;
       if (lane == 0) st_release_gpu(g.progress + kProgStride * ch, J + 1);
       if (g.trace && ch < g.trace_ctas && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * 4 + 1] = global_timer_ns();
+        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 1] = global_timer_ns();
+      if (lane == 0) mbar_arrive(&empty[s]);
     }
     // never leave another CTA waiting on this one
     if (!s_ok && lane == 0) st_release_gpu(g.progress + kProgStride * ch, g.G);
@@ -343,19 +406,27 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     // chunks [first(J), last(J)] (a superset); J needs their progress >=
     // J+1-margin.  seen[] caches the last value read (progress only grows),
     // and the chunks of the next kCheckAhead steps are read along, so most
-    // steps are decided from the cache.
-    auto first_c = [&](uint64_t J) {
-      return ((J * g.g * g.A + i0) / g.B) / g.W;
+    // steps are decided from the cache.  Progress words are read with
+    // gpu-scope acquire loads (each pairs with the owner's release store):
+    // a relaxed read followed by a gpu-scope fence cost about 2 us per step
+    // on this path.
+    // positions below A*B < 2^32: 32-bit divisions by invariants
+    auto first_c = [&](uint64_t J) -> uint64_t {
+      return fdiv(fdiv((uint32_t)(J * g.g * g.A + i0), g.div_Bc), g.div_Wc);
     };
-    auto last_c = [&](uint64_t J) {
+    auto last_c = [&](uint64_t J) -> uint64_t {
       const uint64_t c0 = J * g.g;
       const uint64_t gj = min64(g.g, g.B - c0);
-      return min64((((c0 + gj - 1) * g.A + i0 + Wc - 1) / g.B) / g.W,
+      return min64(fdiv(fdiv((uint32_t)((c0 + gj - 1) * g.A + i0 + Wc - 1),
+                             g.div_Bc),
+                        g.div_Wc),
                    g.nchunks - 1);
     };
     bool good = true;
     for (uint32_t J = 0; J < g.G && good; ++J) {
       const uint32_t s = J % kStages;
+      if (g.trace && ch < g.trace_ctas && lane == 0)
+        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 5] = global_timer_ns();
       const uint32_t need = J + 1 > g.margin ? J + 1 - g.margin : 0u;
       if (need > 0) {
         const uint64_t cf = first_c(J), cl = last_c(J);
@@ -368,7 +439,7 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
             if (seen[c] >= need) continue;
             unsigned ns = 32;
             uint32_t v;
-            while ((v = ld_relaxed_gpu(g.progress + kProgStride * c)) < need) {
+            while ((v = ld_acquire_gpu(g.progress + kProgStride * c)) < need) {
               if (!s_ok || global_timer_ns() - t0 > g.timeout_ns) {
                 good = false;
                 break;
@@ -379,17 +450,18 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
             seen[c] = v;
             loaded = true;
           } else if (seen[c] < need + kCheckAhead) {
-            seen[c] = ld_relaxed_gpu(g.progress + kProgStride * c);
+            seen[c] = ld_acquire_gpu(g.progress + kProgStride * c);
             loaded = true;
           }
         }
         good = __all_sync(kFull, good);
         // relaxed reads followed by this fence act as acquire for every
         // later access of this CTA (the writers' stores come after it)
-        if (__any_sync(kFull, loaded))
-          asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        (void)loaded;
       }
       if (!good) break;
+      if (g.trace && ch < g.trace_ctas && lane == 0)
+        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 4] = global_timer_ns();
       if (J >= kStages) {
         const bool ok = wait_bar(&empty[s], ((J / kStages) - 1) & 1);
         if (!__all_sync(kFull, ok)) {
@@ -398,7 +470,7 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
         }
       }
       if (g.trace && ch < g.trace_ctas && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * 4 + 2] = global_timer_ns();
+        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 2] = global_timer_ns();
       if (lane == 0) mbar_arrive(&ready[s]);
     }
     if (!good && lane == 0) {
@@ -453,7 +525,7 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
       }
       __syncwarp();
       if (g.trace && ch < g.trace_ctas && wid == 0 && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * 4 + 3] = global_timer_ns();
+        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 3] = global_timer_ns();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
   }
@@ -542,10 +614,11 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
       p.smem_bytes = (size_t)smem;
       p.ctas_per_sm = per_sm;
       p.margin = margin;
+      p.A = A;
       uint64_t total = 0;
-      for (uint64_t J = 0; J < G; ++J)
-        total += stash_rows(J, g, A, B, margin);
-      p.stash_bytes = (size_t)(total * g * U);
+      for (uint64_t i = 0; i < A; ++i)
+        total += stash_slot_bytes(i, g, A, B, G, U, margin);
+      p.stash_bytes = (size_t)total;
       return p;
     }
   }
@@ -555,7 +628,7 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
 static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
 size_t stash_zero_offset(const StashPlan &p) {
-  return align256(p.stash_bytes) + align256((size_t)(p.G + 1) * 8);
+  return align256(p.stash_bytes) + align256((size_t)(p.A + 1) * 8);
 }
 
 size_t stash_zero_bytes(const StashPlan &p) {
@@ -563,8 +636,8 @@ size_t stash_zero_bytes(const StashPlan &p) {
 }
 
 size_t stash_scratch_bytes(const StashPlan &p) {
-  // stash + offsets (G+1) + progress counters + status
-  return p.stash_bytes + 256 + (size_t)(p.G + 1) * 8 + 256 +
+  // stash + row offsets (A+1) + progress counters + status
+  return p.stash_bytes + 256 + (size_t)(p.A + 1) * 8 + 256 +
          (size_t)p.nchunks * 4 * kProgStride + 256 + 4;
 }
 
@@ -573,19 +646,18 @@ static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   cudaError_t err;
   {
     ProfScope ps(s, "stash_offsets");
-    k_stash_offsets<<<1, 1024, 0, s>>>(const_cast<uint64_t *>(g.soff), g.A,
-                                       g.B, g.g, g.G, (uint64_t)g.g * g.b * E,
-                                       g.margin);
+    k_stash_offsets<<<1, 1024, 0, s>>>(g);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
   {
-    const uint64_t rmax = stash_rows(g.G - 1, g.g, g.A, g.B, g.margin);
-    if (rmax > 0) {
-      dim3 grid((unsigned)((rmax + kSaveRows - 1) / kSaveRows), g.G);
-      ProfScope ps(s, "stash_save");
-      k_stash_save<E><<<grid, kSaveThreads, 0, s>>>(g);
-      if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    }
+    // rows stashed: those with J_i < G (a prefix of the rows)
+    const DeviceInfo &di = device_info();
+    const uint64_t warps = (g.A + 1) / 2;
+    const unsigned grid = (unsigned)std::min<uint64_t>(
+        (warps * 32 + kSaveThreads - 1) / kSaveThreads, (uint64_t)di.sms * 8);
+    ProfScope ps(s, "stash_save");
+    k_stash_save<<<grid, kSaveThreads, 0, s>>>(g);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
   auto kern = k_stash_wave<E>;
   err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -606,7 +678,7 @@ static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   uint64_t *trace = nullptr;
   if (tr && atoi(tr) > 0) {
     g.trace_ctas = (uint32_t)std::min(atoi(tr), (int)p.nchunks);
-    const size_t tb = (size_t)g.trace_ctas * g.G * 4 * 8;
+    const size_t tb = (size_t)g.trace_ctas * g.G * kTraceSlots * 8;
     if (cudaMalloc(&trace, tb) == cudaSuccess) {
       cudaMemsetAsync(trace, 0, tb, s);
       g.trace = trace;
@@ -620,24 +692,29 @@ static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   if (err != cudaSuccess) return err;
   if (trace) {
     cudaStreamSynchronize(s);
-    const size_t n = (size_t)g.trace_ctas * g.G * 4;
+    const size_t n = (size_t)g.trace_ctas * g.G * kTraceSlots;
     uint64_t *h = (uint64_t *)malloc(n * 8);
     cudaMemcpy(h, trace, n * 8, cudaMemcpyDeviceToHost);
     for (uint32_t c = 0; c < g.trace_ctas; ++c) {
-      double land = 0, deps = 0, wr = 0, per = 0;
-      uint64_t *t = h + (size_t)c * g.G * 4;
+      double land = 0, deps = 0, wr = 0, per = 0, chk = 0, ring = 0, lead = 0;
+      uint64_t *t = h + (size_t)c * g.G * kTraceSlots;
+      auto at = [&](uint32_t J, int k) { return t[J * kTraceSlots + k]; };
+      auto d = [](uint64_t a, uint64_t b) { return (double)(int64_t)(a - b); };
       for (uint32_t J = 1; J + 1 < g.G; ++J) {
-        auto d = [](uint64_t a, uint64_t b) { return (double)(int64_t)(a - b); };
-        land += d(t[J * 4 + 1], t[J * 4 + 0]);
-        deps += d(t[J * 4 + 2], t[J * 4 + 1]);
-        wr += d(t[J * 4 + 3], std::max(t[J * 4 + 2], t[J * 4 + 1]));
-        per += d(t[(J + 1) * 4 + 3], t[J * 4 + 3]);
+        land += d(at(J, 1), at(J, 0));
+        deps += d(at(J, 2), at(J, 1));
+        wr += d(at(J, 3), std::max(at(J, 2), at(J, 1)));
+        per += d(at(J + 1, 3), at(J, 3));
+        chk += d(at(J, 4), at(J, 5));
+        ring += d(at(J, 2), at(J, 4));
+        lead += d(at(J, 1), at(J, 5));
       }
       const double k = (double)(g.G - 2) * 1000.0;
-      fprintf(stderr, "stash trace cta %u: issue->published %.2f us, published->deps ok %.2f us, "
-              "ready->written %.2f us, step period %.2f us, total %.1f us\n", c, land / k,
-              deps / k, wr / k, per / k,
-              (double)(t[(g.G - 1) * 4 + 3] - t[0]) / 1000.0);
+      fprintf(stderr, "stash trace cta %u: issue->published %.2f us, published->ready %.2f us, "
+              "ready->written %.2f us, step period %.2f us; checker: begun %.2f us before "
+              "publish, deps %.2f us, ring %.2f us; total %.1f us\n", c, land / k,
+              deps / k, wr / k, per / k, lead / k, chk / k, ring / k,
+              (double)(at(g.G - 1, 3) - at(0, 0)) / 1000.0);
     }
     free(h);
     cudaFree(trace);
@@ -656,13 +733,14 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   g.base = reinterpret_cast<char *>(buf);
   g.stash = sc;
   size_t off = align(p.stash_bytes);
-  g.soff = reinterpret_cast<const uint64_t *>(sc + off);
-  off += align((size_t)(p.G + 1) * 8);
+  g.roff = reinterpret_cast<const uint64_t *>(sc + off);
+  off += align((size_t)(A + 1) * 8);
   g.progress = reinterpret_cast<uint32_t *>(sc + off);
   g.status = status;
   g.A = A;
   g.B = B;
   g.b = b;
+  g.e = (uint32_t)e;
   g.g = p.g;
   g.G = p.G;
   g.W = p.W;
@@ -675,6 +753,10 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   g.trace = nullptr;
   g.trace_ctas = 0;
   g.margin = p.margin;
+  g.gAk = (uint64_t)p.g * A * p.margin;
+  g.div_D = make_fastdiv((uint32_t)((uint64_t)p.g * (A - 1)));
+  g.div_Bc = make_fastdiv((uint32_t)B);
+  g.div_Wc = make_fastdiv(p.W);
   {
     const char *gm = getenv("LM_STASH_GATHER");
     g.tma = (gm && gm[0] == 'c') ? 0u : 1u;  // "cpasync" selects cp.async

@@ -81,9 +81,11 @@ def main(argv=None) -> int:
     lm.prof_enable(False)
     ms = e0.elapsed_time(e1) / max(args.reps, 1)
     prof = lm.prof_collect()
+    status = int(lm.lib().lm_device_status(None))  # non-zero: a wait timed out
     print(json.dumps({
         "op": args.op, "dims": d, "elem_bytes": e, "payload_bytes": nbytes,
         "ms": round(ms, 4), "GBps_2x": round(2 * nbytes / ms / 1e6, 1),
+        "status": status,
         "kernels": {k: {"launches": v[0], "avg_ms": round(v[1] / v[0], 4)}
                     for k, v in prof.items()}}), flush=True)
     return 0
