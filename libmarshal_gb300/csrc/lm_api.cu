@@ -577,6 +577,7 @@ void lm_marshal_finalize(void) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return;
   cycle_cache_clear();
+  stash_cache_clear();
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
     cudaMemPoolTrimTo(pool, 0);

@@ -95,6 +95,8 @@ size_t stash_scratch_bytes(const StashPlan &p);  // scratch to pass
 // progress counters); the rest is fully written before it is read.
 size_t stash_zero_offset(const StashPlan &p);
 size_t stash_zero_bytes(const StashPlan &p);
+// Frees the cached stash row-offset tables of the current device.
+void stash_cache_clear();
 cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
                             uint64_t B, uint32_t b, const StashPlan &p,
                             void *scratch, uint32_t *status,

@@ -32,6 +32,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "lm_core.cuh"
 #include "lm_internal.h"
@@ -431,7 +434,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
       if (need > 0) {
         const uint64_t cf = first_c(J), cl = last_c(J);
         const uint64_t la = last_c(min64(J + kCheckAhead, g.G - 1));
-        bool loaded = false;
         const uint64_t t0 = global_timer_ns();
         for (uint64_t c = cf + lane; c <= la && good; c += 32) {
           if (c == ch) continue;
@@ -448,16 +450,11 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
               if (ns < 256) ns <<= 1;
             }
             seen[c] = v;
-            loaded = true;
           } else if (seen[c] < need + kCheckAhead) {
             seen[c] = ld_acquire_gpu(g.progress + kProgStride * c);
-            loaded = true;
           }
         }
         good = __all_sync(kFull, good);
-        // relaxed reads followed by this fence act as acquire for every
-        // later access of this CTA (the writers' stores come after it)
-        (void)loaded;
       }
       if (!good) break;
       if (g.trace && ch < g.trace_ctas && lane == 0)
@@ -641,14 +638,105 @@ size_t stash_scratch_bytes(const StashPlan &p) {
          (size_t)p.nchunks * 4 * kProgStride + 256 + 4;
 }
 
+// The row-offset table depends only on the shape, the plan and the buffer
+// address modulo 16: tables computed outside stream capture are kept per
+// device (at most kRoffEntries, kRoffBytes in all) and reused; a call on
+// another stream waits for the producing kernel.
+constexpr int kRoffEntries = 16;
+constexpr size_t kRoffBytes = 64ull << 20;
+struct RoffEntry {
+  void *mem = nullptr;
+  size_t bytes = 0;
+  cudaEvent_t ready = nullptr;
+  uint64_t used = 0;
+};
+using RoffKey = std::tuple<int, uint64_t, uint64_t, uint32_t, uint32_t,
+                           uint32_t, uint32_t, uint32_t>;
+static std::mutex g_roff_mu;
+static std::map<RoffKey, RoffEntry> g_roff;
+static uint64_t g_roff_clock = 0;
+
+static cudaError_t launch_offsets(cudaStream_t s, const StashArgs &g) {
+  ProfScope ps(s, "stash_offsets");
+  k_stash_offsets<<<1, 1024, 0, s>>>(g);
+  return cudaGetLastError();
+}
+
+// Points g.roff at a cached table (computing it on a miss), or computes
+// the table into the caller's scratch while the stream is being captured.
+static cudaError_t stash_offsets(cudaStream_t s, StashArgs &g) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  if (cs != cudaStreamCaptureStatusNone) return launch_offsets(s, g);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const RoffKey key{dev, g.A, g.B, g.b, g.e, g.g, g.margin,
+                    (uint32_t)((uintptr_t)g.base & 15)};
+  std::lock_guard<std::mutex> lock(g_roff_mu);
+  auto it = g_roff.find(key);
+  if (it != g_roff.end()) {
+    it->second.used = ++g_roff_clock;
+    g.roff = reinterpret_cast<const uint64_t *>(it->second.mem);
+    return cudaStreamWaitEvent(s, it->second.ready, 0);
+  }
+  const size_t bytes = (size_t)(g.A + 1) * 8;
+  if (bytes > kRoffBytes) return launch_offsets(s, g);
+  size_t total = bytes;
+  for (auto &kv : g_roff) total += kv.second.bytes;
+  while (!g_roff.empty() &&
+         ((int)g_roff.size() >= kRoffEntries || total > kRoffBytes)) {
+    auto lru = g_roff.begin();
+    for (auto j = g_roff.begin(); j != g_roff.end(); ++j)
+      if (j->second.used < lru->second.used) lru = j;
+    cudaEventSynchronize(lru->second.ready);
+    cudaFree(lru->second.mem);  // waits for every reader
+    cudaEventDestroy(lru->second.ready);
+    total -= lru->second.bytes;
+    g_roff.erase(lru);
+  }
+  RoffEntry en;
+  en.bytes = bytes;
+  cudaError_t err = cudaMalloc(&en.mem, bytes);
+  if (err != cudaSuccess) return launch_offsets(s, g);  // scratch fallback
+  if ((err = cudaEventCreateWithFlags(&en.ready, cudaEventDisableTiming)) !=
+      cudaSuccess) {
+    cudaFree(en.mem);
+    return err;
+  }
+  StashArgs gc = g;
+  gc.roff = reinterpret_cast<const uint64_t *>(en.mem);
+  if ((err = launch_offsets(s, gc)) != cudaSuccess ||
+      (err = cudaEventRecord(en.ready, s)) != cudaSuccess) {
+    cudaFree(en.mem);
+    cudaEventDestroy(en.ready);
+    return err;
+  }
+  en.used = ++g_roff_clock;
+  g_roff[key] = en;
+  g.roff = gc.roff;
+  return cudaSuccess;
+}
+
+void stash_cache_clear() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(g_roff_mu);
+  for (auto it = g_roff.begin(); it != g_roff.end();) {
+    if (std::get<0>(it->first) != dev) {
+      ++it;
+      continue;
+    }
+    cudaEventSynchronize(it->second.ready);
+    cudaFree(it->second.mem);
+    cudaEventDestroy(it->second.ready);
+    it = g_roff.erase(it);
+  }
+}
+
 template <int E>
 static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   cudaError_t err;
-  {
-    ProfScope ps(s, "stash_offsets");
-    k_stash_offsets<<<1, 1024, 0, s>>>(g);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
-  }
+  if ((err = stash_offsets(s, g)) != cudaSuccess) return err;
   {
     // rows stashed: those with J_i < G (a prefix of the rows)
     const DeviceInfo &di = device_info();
