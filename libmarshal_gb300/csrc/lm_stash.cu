@@ -588,12 +588,7 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
     const uint32_t pitch = stash_pitch(g * U, e);
     for (int per_sm : per_sms) {
       const uint64_t ctas = (uint64_t)di.sms * per_sm;
-      // rows per chunk a multiple of 8 (when that still leaves >= 3/4 of
-      // the CTAs busy), so each chunk's output segments start on 32-byte
-      // sectors and the writers' 8-row patches stay whole
-      uint64_t W = (A + ctas - 1) / ctas;
-      const uint64_t W8 = (W + 7) / 8 * 8;
-      if ((A + W8 - 1) / W8 * 4 >= ctas * 3) W = W8;
+      const uint64_t W = (A + ctas - 1) / ctas;
       const uint64_t smem = (uint64_t)kStages * stash_stage_bytes(W, pitch);
       if (smem > max_smem / per_sm) continue;
       if (W * g * b >= 0xffffffffull || g * b >= 0xffffffffull) continue;
