@@ -41,9 +41,11 @@ CONFIG = {
     "l2": "inputs larger than L2 (805 MB vs 126 MB); no flush needed",
     "steps_alternate": "(16384,12289) then (12289,16384)",
 }
-# DRAM traffic of the dominant kernel per launch, from one ncu capture
-# (profiles/); None until captured.
-NCU_TRAFFIC = {}
+# DRAM traffic of the dominant kernel per launch (dram__bytes_read.sum +
+# dram__bytes_write.sum), from one ncu capture of k_stash_wave on the
+# forward 100(16384, 12289) fp32 call (profiles/stash_wave_save_100_16384x
+# 12289_f32.txt): 809.7 MB read + 754.1 MB written.
+NCU_TRAFFIC = {"stash_wave": 1563818752}
 
 
 def peak_hbm():
