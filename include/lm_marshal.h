@@ -101,7 +101,9 @@ bool lm_transpose_0100(lm_stream_t stream, void *buf, int elem_bytes, int A,
  * is overwritten first, then a streaming wavefront), 4 = two passes (BS on
  * tiles that make >= 128-byte units, then PTTWAC on those units), 5 = whole
  * cycles (when every cycle of 100(a, B) has at most 32 units: find each
- * cycle's smallest position, then move whole cycles through registers).  Returns
+ * cycle's smallest position, then move whole cycles through registers),
+ * 6 = through scratch (each tile's blocks transposed out of place into a
+ * stream-ordered scratch buffer of the payload's size, then copied back).  Returns
  * true when the forced algorithm does not apply to the shape.  No reference
  * counterpart (the reference picks by super-element size,
  * cl_marshal.cc:365-370). */

@@ -100,6 +100,19 @@ struct Scratch {
   }
 };
 
+// Like get_scratch, but a failed allocation only returns false (no error
+// recorded): for plans that have a fallback.
+static bool try_scratch(Scratch &sc, size_t bytes, cudaStream_t s) {
+  pool_keep_memory();
+  sc.s = s;
+  if (cudaMallocAsync(&sc.p, bytes ? bytes : 4, s) != cudaSuccess) {
+    cudaGetLastError();
+    sc.p = nullptr;
+    return false;
+  }
+  return true;
+}
+
 static bool get_scratch(Scratch &sc, size_t bytes, cudaStream_t s) {
   pool_keep_memory();
   sc.s = s;
@@ -203,7 +216,7 @@ static uint64_t wait_timeout_ns() {
 
 // ---- planner ----------------------------------------------------------------
 
-enum class Method { Auto, BS, Pttwac, Stash, TwoPass, Cycles };
+enum class Method { Auto, BS, Pttwac, Stash, TwoPass, Cycles, Staged };
 
 static bool check_launch(cudaError_t e, const char *what) {
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -282,22 +295,25 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
       cudaStreamIsCapturing(s, &cs);
       Scratch sc;
-      if (cs != cudaStreamCaptureStatusNone &&
-          get_scratch(sc, cycle_scratch_bytes(a, B), s))
-        return true;
-      return check_launch(launch_cycles100(s, buf, e, T, (uint32_t)a,
-                                           (uint32_t)B, (uint32_t)b, L, sc.p),
-                          "cycles launch");
+      if (get_scratch(sc, cycle_scratch_bytes(a, B), s)) return true;
+      return check_launch(
+          launch_cycles100(s, buf, e, T, (uint32_t)a, (uint32_t)B,
+                           (uint32_t)b, L, sc.p,
+                           cs == cudaStreamCaptureStatusNone),
+          "cycles launch");
     }
     if (m == Method::Cycles)
       return fail("cycles: the cycles of 100(%llu, %llu) are longer than %u",
                   (unsigned long long)a, (unsigned long long)B,
                   (unsigned)kCycleMaxLen);
   }
+  // the stash wavefront spreads rows over all CTAs: with fewer than 8 rows
+  // per CTA (two per SM) its steps are too small to keep HBM busy
+  const uint64_t stash_min_rows = 16ull * (uint64_t)device_info().sms;
   const bool want_stash =
       m == Method::Stash ||
       (m == Method::Auto && T == 1 && U < 128 && a * B >= (1ull << 20) &&
-       !getenv("LM_NO_STASH"));
+       a >= stash_min_rows && !getenv("LM_NO_STASH"));
   if (want_stash) {
     // 100 on small units: the 3 x payload streaming plan (lm_stash.cu).
     StashPlan sp = T == 1 ? plan_stash(a, B, (uint32_t)b, e) : StashPlan();
@@ -316,6 +332,22 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
       return fail("stash plan not applicable to 0100(%llu, %llu, %llu, %llu)",
                   (unsigned long long)T, (unsigned long long)a,
                   (unsigned long long)B, (unsigned long long)b);
+  }
+  // any shape through scratch: block transposes out of place, then a copy
+  // back (4 x payload, but every access in whole sectors); falls through
+  // when the scratch cannot be had
+  if (m == Method::Staged ||
+      (m == Method::Auto && T * a * B * b * e >= (1ull << 20) &&
+       !getenv("LM_NO_STAGED"))) {
+    if (staged0100_applies(T, a, B, b, e)) {
+      Scratch sc;
+      if (try_scratch(sc, T * a * B * b * e, s))
+        return check_launch(launch_staged0100(s, buf, e, T, a, B, b, sc.p),
+                            "staged launch");
+      if (m == Method::Staged) return fail("staged: no scratch for this size");
+    } else if (m == Method::Staged) {
+      return fail("staged: units above 32 KB or too many blocks");
+    }
   }
   if ((m == Method::Auto && U < 128) || m == Method::TwoPass) {
     // Aggregate small super-elements into >=128-byte units first so the
@@ -402,6 +434,8 @@ static bool method_applies(Method m, int e, uint64_t T, uint64_t a,
       return plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e).feasible;
     case Method::Cycles:
       return cycle_order(a, B, kCycleMaxLen) != 0 && a * B - 1 <= (1ull << 28);
+    case Method::Staged:
+      return staged0100_applies(T, a, B, b, e);
     default:
       return true;
   }
@@ -417,9 +451,10 @@ static Method tuned_method(cudaStream_t s, int e, uint64_t T, uint64_t a,
     if (it != g_tune.end()) return (Method)it->second;
   }
   const uint64_t bytes = T * a * B * b * (uint64_t)e;
-  Method cand[5];
+  Method cand[6];
   int nc = 0;
   cand[nc++] = Method::Auto;
+  if (method_applies(Method::Staged, e, T, a, B, b)) cand[nc++] = Method::Staged;
   if (method_applies(Method::Cycles, e, T, a, B, b)) cand[nc++] = Method::Cycles;
   if (T == 1 && plan_stash(a, B, (uint32_t)b, e).feasible) cand[nc++] = Method::Stash;
   if (b * e < 128 && (split_a(a, B, b, e) || split_B(a, B, b, e)))
@@ -632,12 +667,13 @@ bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
                               unsigned long long *et) {
   OpTimer t(et, (cudaStream_t)stream);
   if (A < 0 || a < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
-  if (method < 0 || method > 5) return fail("method must be 0..5");
+  if (method < 0 || method > 6) return fail("method must be 0..6");
   const Method m = method == 1   ? Method::BS
                    : method == 2 ? Method::Pttwac
                    : method == 3 ? Method::Stash
                    : method == 4 ? Method::TwoPass
                    : method == 5 ? Method::Cycles
+                   : method == 6 ? Method::Staged
                                  : Method::Auto;
   if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
               (uint64_t)B, (uint64_t)b, m))

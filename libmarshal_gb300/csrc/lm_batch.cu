@@ -72,6 +72,9 @@ struct BatchArgs {
   uint32_t *counter;
   uint32_t *status;  // set to kStatusWaitTimeout if a staged load never lands
   uint32_t stage_bytes;  // staged gather: bytes of one shared-memory stage
+  // staged gather of one job without tables (items == nullptr): blocks
+  // 0 .. nitems-1 of `single`, taken by the CTAs in a fixed stride
+  BJob single;
 };
 
 template <int E>
@@ -506,8 +509,18 @@ __global__ void __launch_bounds__(kStageThreads, 3) k_batch_gather(BatchArgs g) 
   __shared__ int s_dead;
   __shared__ __align__(16) BJob s_jobs[2];  // job of the block in each stage
   const uint32_t warp = threadIdx.x >> 5;
+  const BJob *jobs = g.items ? g.jobs : &g.single;
   uint32_t c_job = 0, c_q = 0, c_end = 0;  // thread 0's cursor
+  bool c_first = true;
   auto fetch = [&](int slot) {
+    if (!g.items) {
+      c_q = c_first ? blockIdx.x : c_q + gridDim.x;
+      c_first = false;
+      s_valid[slot] = c_q < g.nitems;
+      s_job[slot] = 0;
+      s_q[slot] = c_q;
+      return;
+    }
     if (c_q >= c_end) {
       const uint32_t k = atomicAdd(g.counter, 1u);
       if (k >= g.nitems) {
@@ -534,8 +547,8 @@ __global__ void __launch_bounds__(kStageThreads, 3) k_batch_gather(BatchArgs g) 
   if (!s_valid[0]) return;
   uint32_t cq = s_q[0];
   if (warp == 0) {
-    copy_job(&s_jobs[0], &g.jobs[s_job[0]]);
-    gather_issue(g.jobs[s_job[0]], cq, smem, rowoff[0], &bar[0]);
+    copy_job(&s_jobs[0], &jobs[s_job[0]]);
+    gather_issue(jobs[s_job[0]], cq, smem, rowoff[0], &bar[0]);
   }
   uint32_t parity = 0;   // bit st: phase to wait for on bar[st]
   uint32_t pending = 1;  // bit st: loads issued to stage st, not yet seen
@@ -548,8 +561,8 @@ __global__ void __launch_bounds__(kStageThreads, 3) k_batch_gather(BatchArgs g) 
     const uint32_t nj = s_job[nx], nq = s_q[nx];
     if (more) {
       if (warp == 0) {
-        copy_job(&s_jobs[nx], &g.jobs[nj]);
-        gather_issue(g.jobs[nj], nq, smem + (size_t)nx * g.stage_bytes,
+        copy_job(&s_jobs[nx], &jobs[nj]);
+        gather_issue(jobs[nj], nq, smem + (size_t)nx * g.stage_bytes,
                      rowoff[nx], &bar[nx]);
       }
       pending |= 1u << nx;
@@ -863,6 +876,38 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.bytes = 0;
 }
 
+// Staged form of a job: S x S unit blocks (S the largest power of two up to
+// 128 with S*S units in kStageTileBytes), rows staged as 16-byte aligned
+// supersets at an odd number of 16-byte words.  False when a unit exceeds
+// kStageTileBytes or the job has 2^32 blocks or more.  `scratch` is left
+// for the caller.
+static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
+                       uint64_t *nblk, size_t *stage_bytes) {
+  const uint64_t unit = nz.b * (uint64_t)jb.elem_bytes;
+  if (unit > kStageTileBytes || nz.a * nz.B * nz.b >= 0xffffffffull)
+    return false;
+  uint32_t S = 128;
+  while (S > 1 && (uint64_t)S * S * unit > kStageTileBytes) S >>= 1;
+  const uint64_t nI = (nz.a + S - 1) / S, nJ = (nz.B + S - 1) / S;
+  if (nz.T * nI * nJ >= 0xffffffffull) return false;
+  uint32_t sp = (uint32_t)((S * unit + 15) / 16 * 16 + 16);
+  if (((sp / 16) & 1) == 0) sp += 16;  // rows in distinct bank groups
+  fill_job(j, jb, nz, sp);
+  j.S = S;
+  j.ng8 = (S + 7) / 8;
+  j.div_ng8 = make_fastdiv(j.ng8);
+  j.nJ = (uint32_t)nJ;
+  j.nIJ = (uint32_t)(nI * nJ);
+  j.div_Sb = make_fastdiv(S * (uint32_t)nz.b);
+  j.div_nJ = make_fastdiv(j.nJ);
+  j.div_nIJ = make_fastdiv(j.nIJ);
+  j.bytes = nz.T * nz.a * nz.B * nz.b * (uint64_t)jb.elem_bytes;
+  *nblk = nz.T * nI * nJ;
+  *stage_bytes = ((size_t)S * sp + 127) / 128 * 128;
+  return true;
+}
+
+
 // Host planning of a job list into small items, big items, cluster items and
 // large jobs.
 static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
@@ -992,30 +1037,15 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
         }
         {
           const int w = bt->nwaves - 1;
-          uint32_t S = 128;
-          while (S > 1 && (uint64_t)S * S * unit > kStageTileBytes) S >>= 1;
-          const uint64_t nI = (nz.a + S - 1) / S, nJ = (nz.B + S - 1) / S;
-          if (nz.T * nI * nJ >= 0xffffffffull) goto planner;
           BJob j;
-          // staged rows: 16-byte aligned supersets of S-unit segments
-          uint32_t sp = (uint32_t)((S * unit + 15) / 16 * 16 + 16);
-          if (((sp / 16) & 1) == 0) sp += 16;  // rows in distinct bank groups
-          fill_job(j, jb, nz, sp);
-          j.S = S;
-          j.ng8 = (S + 7) / 8;
-          j.div_ng8 = make_fastdiv(j.ng8);
-          j.nJ = (uint32_t)nJ;
-          j.nIJ = (uint32_t)(nI * nJ);
-          j.div_Sb = make_fastdiv(S * (uint32_t)nz.b);
-          j.div_nJ = make_fastdiv(j.nJ);
-          j.div_nIJ = make_fastdiv(j.nIJ);
-          j.bytes = bytes;
+          uint64_t nblk = 0;
+          size_t stage = 0;
+          if (!staged_job(j, jb, nz, &nblk, &stage)) goto planner;
           // same address modulo 16 as the buffer (see k_batch_copyback);
           // the arena base is set when the wave is enqueued
           j.scratch = (char *)(uintptr_t)(wave_used + ((uintptr_t)jb.buf & 15));
           const uint32_t jid = (uint32_t)bt->jobs.size();
           bt->jobs.push_back(j);
-          const uint64_t nblk = nz.T * nI * nJ;
           for (uint64_t q = 0; q < nblk; q += kStageBlocksPerItem) {
             BItem it;
             it.job = jid;
@@ -1031,8 +1061,7 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
             it.ntiles = 0;
             bt->wcopy[w].push_back(it);
           }
-          bt->wsmem[w] =
-              std::max<size_t>(bt->wsmem[w], ((size_t)S * sp + 127) / 128 * 128);
+          bt->wsmem[w] = std::max<size_t>(bt->wsmem[w], stage);
           wave_used += foot;
           bt->need_arena = std::max(bt->need_arena, wave_used);
           bt->stats.staged_jobs += 1;
@@ -1148,6 +1177,76 @@ static bool launch_staged(cudaStream_t s, const BJob *d_jobs,
   if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
   return false;
 }
+
+namespace lm {
+
+bool staged0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
+                        int e) {
+  lm_job jb{};
+  jb.elem_bytes = e;
+  Normalized nz;
+  nz.ok = true;
+  nz.T = T;
+  nz.a = a;
+  nz.B = B;
+  nz.b = b;
+  BJob j;
+  uint64_t nblk;
+  size_t stage;
+  return T > 0 && a > 1 && B > 1 && b > 0 &&
+         staged_job(j, jb, nz, &nblk, &stage);
+}
+
+// One 0100 through scratch: the staged gather writes the transposed blocks
+// to `scratch` (T*a*B*b*e bytes), then a device-to-device copy brings them
+// back over the buffer.
+cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
+                              uint64_t a, uint64_t B, uint64_t b,
+                              void *scratch) {
+  lm_job jb{};
+  jb.buf = buf;
+  jb.elem_bytes = e;
+  Normalized nz;
+  nz.ok = true;
+  nz.T = T;
+  nz.a = a;
+  nz.B = B;
+  nz.b = b;
+  BatchArgs g{};
+  uint64_t nblk = 0;
+  size_t stage = 0;
+  if (!staged_job(g.single, jb, nz, &nblk, &stage)) return cudaErrorInvalidValue;
+  g.single.scratch = reinterpret_cast<char *>(scratch);
+  const size_t dyn = 2 * stage;
+  cudaError_t err = cudaSuccess;
+  if (dyn > 48 * 1024 &&
+      (err = cudaFuncSetAttribute(k_batch_gather,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)dyn)) != cudaSuccess)
+    return err;
+  int occ = 0;
+  if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+           &occ, k_batch_gather, kStageThreads, dyn)) != cudaSuccess)
+    return err;
+  const DeviceInfo &di = device_info();
+  const uint32_t grid = (uint32_t)std::min<uint64_t>(
+      (uint64_t)di.sms * std::max(occ, 1), nblk);
+  g.jobs = nullptr;
+  g.items = nullptr;
+  g.nitems = (uint32_t)nblk;
+  g.counter = nullptr;
+  g.status = device_status_word();
+  g.stage_bytes = (uint32_t)stage;
+  {
+    ProfScope ps(s, "staged_gather");
+    k_batch_gather<<<grid, kStageThreads, dyn, s>>>(g);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  return cudaMemcpyAsync(buf, scratch, g.single.bytes, cudaMemcpyDeviceToDevice,
+                         s);
+}
+
+}  // namespace lm
 
 static bool launch_items(cudaStream_t s, const BJob *d_jobs,
                          const BItem *d_items, uint32_t nitems,

@@ -180,19 +180,18 @@ cudaError_t launch_move(cudaStream_t s, char *base, uint64_t T,
 }
 
 // Cycle leaders depend only on (a, B): lists computed outside stream capture
-// are kept per device (at most kCacheEntries lists, kCacheBytes in all) and
-// reused; a later call on another stream waits for the producing kernel.
+// are kept per device (the first kCacheEntries shapes, kCacheBytes in all,
+// until lm_marshal_finalize) and reused; a later call on another stream
+// waits for the producing kernel.
 constexpr int kCacheEntries = 16;
 constexpr size_t kCacheBytes = 512ull << 20;
 struct CycEntry {
   void *mem = nullptr;  // count word + list
   size_t bytes = 0;
   cudaEvent_t ready = nullptr;
-  uint64_t used = 0;
 };
 std::mutex g_cyc_mu;
 std::map<std::tuple<int, uint64_t, uint64_t>, CycEntry> g_cyc;
-uint64_t g_cyc_clock = 0;
 
 }  // namespace
 
@@ -233,43 +232,40 @@ static cudaError_t run_leaders(cudaStream_t s, uint32_t a, const ModM &m,
   return cudaGetLastError();
 }
 
-// The leader list of 100(a, B): from the cache, or computed into `scratch`
-// (during stream capture), or computed into a new cache entry.
+// The leader list of 100(a, B): from the cache, or computed into a new
+// cache entry, or (during stream capture, or with the cache full) computed
+// into `scratch`.
 static cudaError_t leaders_for(cudaStream_t s, uint32_t a, uint32_t B,
                                const ModM &m, uint32_t L, bool w32,
-                               void *scratch, void **mem) {
-  if (scratch) {
+                               void *scratch, bool may_cache, void **mem) {
+  auto into_scratch = [&]() {
     *mem = scratch;
     return run_leaders(s, a, m, L, w32, scratch);
-  }
+  };
+  if (!may_cache) return into_scratch();
   int dev = 0;
   cudaGetDevice(&dev);
   const auto key = std::make_tuple(dev, (uint64_t)a, (uint64_t)B);
   std::lock_guard<std::mutex> lock(g_cyc_mu);
   auto it = g_cyc.find(key);
   if (it != g_cyc.end()) {
-    it->second.used = ++g_cyc_clock;
     *mem = it->second.mem;
     return cudaStreamWaitEvent(s, it->second.ready, 0);
   }
   const size_t bytes = cycle_scratch_bytes(a, B);
+  // a full cache admits nothing more (no eviction: freeing device memory
+  // would synchronise the device); other shapes use per-call memory
   size_t total = bytes;
   for (auto &kv : g_cyc) total += kv.second.bytes;
-  while (!g_cyc.empty() &&
-         ((int)g_cyc.size() >= kCacheEntries || total > kCacheBytes)) {
-    auto lru = g_cyc.begin();
-    for (auto j = g_cyc.begin(); j != g_cyc.end(); ++j)
-      if (j->second.used < lru->second.used) lru = j;
-    cudaEventSynchronize(lru->second.ready);
-    cudaFree(lru->second.mem);  // waits for every reader
-    cudaEventDestroy(lru->second.ready);
-    total -= lru->second.bytes;
-    g_cyc.erase(lru);
-  }
+  if ((int)g_cyc.size() >= kCacheEntries || total > kCacheBytes)
+    return into_scratch();
   CycEntry en;
   en.bytes = bytes;
   cudaError_t err = cudaMalloc(&en.mem, bytes);
-  if (err != cudaSuccess) return err;
+  if (err != cudaSuccess) {
+    cudaGetLastError();  // clear the failed allocation's error
+    return into_scratch();
+  }
   if ((err = cudaEventCreateWithFlags(&en.ready, cudaEventDisableTiming)) !=
       cudaSuccess) {
     cudaFree(en.mem);
@@ -281,7 +277,6 @@ static cudaError_t leaders_for(cudaStream_t s, uint32_t a, uint32_t B,
     cudaEventDestroy(en.ready);
     return err;
   }
-  en.used = ++g_cyc_clock;
   g_cyc[key] = en;
   *mem = en.mem;
   return cudaSuccess;
@@ -305,7 +300,7 @@ void cycle_cache_clear() {
 
 cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
                              uint32_t a, uint32_t B, uint32_t b, uint32_t L,
-                             void *scratch) {
+                             void *scratch, bool may_cache) {
   const uint64_t M = (uint64_t)a * B - 1;
   if (L == 0 || L > kCycleMaxLen || M >= (1ull << 32))
     return cudaErrorInvalidValue;
@@ -316,7 +311,7 @@ cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
   const uint32_t U = b * (uint32_t)e;
   const bool w32 = (uint64_t)a * (M - 1) < (1ull << 32);
   void *mem = nullptr;
-  cudaError_t err = leaders_for(s, a, B, m, L, w32, scratch, &mem);
+  cudaError_t err = leaders_for(s, a, B, m, L, w32, scratch, may_cache, &mem);
   if (err != cudaSuccess) return err;
   const uint32_t *count = reinterpret_cast<const uint32_t *>(mem);
   const uint32_t *list =

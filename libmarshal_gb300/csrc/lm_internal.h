@@ -113,12 +113,21 @@ size_t cycle_scratch_bytes(uint64_t a, uint64_t B);
 // their readers).
 void cycle_cache_clear();
 // T instances of 100(a, B, b) whose cycles have at most L <= kCycleMaxLen
-// units.  With `scratch` (cycle_scratch_bytes(a, B) bytes) the cycle leaders
-// are computed there; with nullptr they come from a per-device cache of
-// recent shapes (not to be used while the stream is being captured).
+// units.  `scratch` holds cycle_scratch_bytes(a, B) bytes; with may_cache
+// (never while the stream is being captured) the cycle leaders come from a
+// per-device cache of shapes, else they are computed into the scratch.
 cudaError_t launch_cycles100(cudaStream_t s, void *buf, int e, uint64_t T,
                              uint32_t a, uint32_t B, uint32_t b, uint32_t L,
-                             void *scratch);
+                             void *scratch, bool may_cache);
+
+// ---- 0100 through scratch (lm_batch.cu) -------------------------------------
+// The blocks of every tile transposed through shared memory into `scratch`
+// (T*a*B*b*e bytes, out of place), then copied back over the buffer: 4 x
+// payload traffic, any shape whose unit is at most 32 KB.
+bool staged0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b, int e);
+cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
+                              uint64_t a, uint64_t B, uint64_t b,
+                              void *scratch);
 
 // An LM_OP_* with its dimensions as the 0100(T, a, B, b) it performs; false
 // for an unknown op or bad dimensions (lm_batch.cu).

@@ -635,21 +635,20 @@ size_t stash_scratch_bytes(const StashPlan &p) {
 
 // The row-offset table depends only on the shape, the plan and the buffer
 // address modulo 16: tables computed outside stream capture are kept per
-// device (at most kRoffEntries, kRoffBytes in all) and reused; a call on
-// another stream waits for the producing kernel.
+// device (the first kRoffEntries shapes, kRoffBytes in all, until
+// lm_marshal_finalize) and reused; a call on another stream waits for the
+// producing kernel.
 constexpr int kRoffEntries = 16;
 constexpr size_t kRoffBytes = 64ull << 20;
 struct RoffEntry {
   void *mem = nullptr;
   size_t bytes = 0;
   cudaEvent_t ready = nullptr;
-  uint64_t used = 0;
 };
 using RoffKey = std::tuple<int, uint64_t, uint64_t, uint32_t, uint32_t,
                            uint32_t, uint32_t, uint32_t>;
 static std::mutex g_roff_mu;
 static std::map<RoffKey, RoffEntry> g_roff;
-static uint64_t g_roff_clock = 0;
 
 static cudaError_t launch_offsets(cudaStream_t s, const StashArgs &g) {
   ProfScope ps(s, "stash_offsets");
@@ -670,29 +669,23 @@ static cudaError_t stash_offsets(cudaStream_t s, StashArgs &g) {
   std::lock_guard<std::mutex> lock(g_roff_mu);
   auto it = g_roff.find(key);
   if (it != g_roff.end()) {
-    it->second.used = ++g_roff_clock;
     g.roff = reinterpret_cast<const uint64_t *>(it->second.mem);
     return cudaStreamWaitEvent(s, it->second.ready, 0);
   }
   const size_t bytes = (size_t)(g.A + 1) * 8;
-  if (bytes > kRoffBytes) return launch_offsets(s, g);
+  // a full cache admits nothing more (no eviction: freeing device memory
+  // would synchronise the device); other shapes use per-call scratch
   size_t total = bytes;
   for (auto &kv : g_roff) total += kv.second.bytes;
-  while (!g_roff.empty() &&
-         ((int)g_roff.size() >= kRoffEntries || total > kRoffBytes)) {
-    auto lru = g_roff.begin();
-    for (auto j = g_roff.begin(); j != g_roff.end(); ++j)
-      if (j->second.used < lru->second.used) lru = j;
-    cudaEventSynchronize(lru->second.ready);
-    cudaFree(lru->second.mem);  // waits for every reader
-    cudaEventDestroy(lru->second.ready);
-    total -= lru->second.bytes;
-    g_roff.erase(lru);
-  }
+  if ((int)g_roff.size() >= kRoffEntries || total > kRoffBytes)
+    return launch_offsets(s, g);
   RoffEntry en;
   en.bytes = bytes;
   cudaError_t err = cudaMalloc(&en.mem, bytes);
-  if (err != cudaSuccess) return launch_offsets(s, g);  // scratch fallback
+  if (err != cudaSuccess) {
+    cudaGetLastError();  // clear the failed allocation's error
+    return launch_offsets(s, g);  // into scratch
+  }
   if ((err = cudaEventCreateWithFlags(&en.ready, cudaEventDisableTiming)) !=
       cudaSuccess) {
     cudaFree(en.mem);
@@ -706,7 +699,6 @@ static cudaError_t stash_offsets(cudaStream_t s, StashArgs &g) {
     cudaEventDestroy(en.ready);
     return err;
   }
-  en.used = ++g_roff_clock;
   g_roff[key] = en;
   g.roff = gc.roff;
   return cudaSuccess;

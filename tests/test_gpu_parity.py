@@ -359,19 +359,21 @@ def test_elapsed_time_accumulates(L):
 
 @pytest.mark.parametrize("e", [1, 2, 4, 8])
 def test_every_method_on_medium_100(L, e):
-    # methods: 0 planner, 1 BS (may refuse), 2 PTTWAC, 3 stash, 4 two-pass
+    # methods: 0 planner, 1 BS (may refuse), 2 PTTWAC, 3 stash, 4 two-pass,
+    # 5 whole cycles (refuses long cycles), 6 through scratch
     from libmarshal_gb300.lm import LMError
     shapes = [(2048, 1031, 1), (1031, 2048, 1), (1500, 1200, 3),
-              (4096, 600, 2), (700, 3000, 1), (3000, 700, 5)]
+              (4096, 600, 2), (700, 3000, 1), (3000, 700, 5), (3, 50000, 7),
+              (40000, 37, 1)]
     for (A, B, b) in shapes:
         src = O.random_bits(A * B * b, e, A * 7 + B)
         want = O.t100(src, A, B, b)
-        for method in (0, 1, 2, 3, 4):
+        for method in (0, 1, 2, 3, 4, 5, 6):
             d = to_dev(src)
             try:
                 L.transpose_0100(d, 1, A, B, b, method=method, elem_bytes=e)
             except LMError:
-                assert method in (1, 3, 4), (A, B, b, e, method)
+                assert method in (1, 3, 4, 5), (A, B, b, e, method)
                 continue
             assert np.array_equal(from_dev(d, e), want), (A, B, b, e, method)
     assert L.lib().lm_device_status(None) == 0
@@ -421,3 +423,28 @@ def test_headline_full_size_fp32(L):
 @pytest.mark.slow
 def test_large_fp64_32768x16000(L):
     _full_size_100(L, 32768, 16000, 8, 2025)
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_staged_method_shapes(L, e):
+    """Method 6 (through scratch) on 0100s with several tiles, units of
+    several elements, ragged block edges and a base that is only
+    element-aligned."""
+    import torch
+    rng = np.random.default_rng(60 + e)
+    for _ in range(6):
+        T = int(rng.integers(1, 4))
+        a = int(rng.integers(2, 700))
+        B = int(rng.integers(2, 700))
+        b = int(rng.choice([1, 2, 3, 8]))
+        n = T * a * B * b
+        src = O.random_bits(n, e, T + a + B + b)
+        raw = torch.zeros(n * e + 64, dtype=torch.uint8, device="cuda")
+        view = raw[e:e + n * e]
+        view.copy_(torch.from_numpy(src.view(np.uint8).copy()).cuda())
+        assert not L.lib().lm_transpose_0100_method(
+            None, view.data_ptr(), e, T, a, B, b, 6, None), L.last_error()
+        torch.cuda.synchronize()
+        got = view.cpu().numpy().view(O.DTYPES[e])
+        assert np.array_equal(got, O.t0100(src, T, a, B, b)), (T, a, B, b, e)
+    assert L.lib().lm_device_status(None) == 0
