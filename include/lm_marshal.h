@@ -166,7 +166,7 @@ bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
  * with LM_BATCH_NO_CLUSTER); jobs that fit the batch's scratch arena
  * (LM_BATCH_SCRATCH_MB, default 1024; not with LM_BATCH_NO_SCRATCH) are
  * staged: transposed block by block into the arena, then copied back, in
- * waves of at most one arena each (two launches per wave, at most 8 waves);
+ * waves of at most one arena each (two launches per wave, at most 32 waves);
  * the rest go through the per-op planner, spread over the batch's side
  * streams, whose algorithm choice per shape class is autotuned (timed once
  * on a scratch buffer, then remembered; LM_TUNE_FILE persists the table).  With LM_BATCH_GRAPH, the second run of an identical
@@ -207,6 +207,9 @@ void lm_batch_destroy(lm_batch_t batch);
 bool lm_batch_run(lm_batch_t batch, lm_stream_t stream, const lm_job *jobs,
                   int njobs, unsigned flags);
 bool lm_batch_stats_get(lm_batch_t batch, lm_batch_stats *out);
+/* Bytes of the staging arena of this handle (0: LM_BATCH_SCRATCH_MB, whose
+ * default is 1024 MiB); applies from the next lm_batch_run. */
+bool lm_batch_set_arena(lm_batch_t batch, unsigned long long bytes);
 /* Autotuner table: entries tuned so far (and loaded from LM_TUNE_FILE). */
 int lm_tune_entries(void);
 

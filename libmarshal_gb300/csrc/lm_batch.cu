@@ -32,12 +32,15 @@ namespace lm {
 constexpr int kBatchThreads = 512;
 constexpr uint32_t kSmallItem = 40 * 1024;
 constexpr int kBandGroups = 4;       // clusters of 2, 4, 8 and 16 CTAs
-constexpr int kMaxWaves = 8;         // staged waves per batch
+constexpr int kMaxWaves = 32;        // staged waves per batch
 constexpr int kCounterStride = 32;   // counters 128 bytes apart
 // small, big, one per cluster size, two per staged wave
 constexpr size_t kCounterBytes =
     (size_t)(2 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
 constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
+// jobs at least this large that the stash plan applies to skip the staged
+// form (the stash moves 3 x payload, the staged form 4 x)
+constexpr uint64_t kStashPreferBytes = 64ull << 20;
 constexpr int kSideStreams = 5;      // streams of the large jobs and groups
 
 struct BJob {
@@ -77,62 +80,157 @@ struct BatchArgs {
   BJob single;
 };
 
+// Warp 0: copies a job descriptor into shared memory (read there by every
+// thread instead of being held in registers).
+__device__ __forceinline__ void copy_job(BJob *dst, const BJob *src) {
+  static_assert(sizeof(BJob) % 4 == 0, "BJob is copied in 32-bit words");
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t k = lane; k < sizeof(BJob) / 4; k += 32)
+    reinterpret_cast<uint32_t *>(dst)[k] =
+        reinterpret_cast<const uint32_t *>(src)[k];
+}
+
+// Element k (a compile-time index after unrolling) of a 16-byte vector, and
+// its replacement, for E-byte elements.
+template <int E>
+__device__ __forceinline__ typename Elem<E>::T vec_elem(const uint4 &x,
+                                                        uint32_t k) {
+  const uint32_t w = k * E / 4;  // 32-bit word holding the element
+  const uint32_t word = w == 0 ? x.x : w == 1 ? x.y : w == 2 ? x.z : x.w;
+  if (E == 8) {
+    const uint32_t hi = w == 0 ? x.y : w == 2 ? x.w : 0u;
+    return (typename Elem<E>::T)(((uint64_t)hi << 32) | word);
+  }
+  if (E == 4) return (typename Elem<E>::T)word;
+  const uint32_t sh = (k * E % 4) * 8;
+  return (typename Elem<E>::T)(word >> sh);
+}
+
+template <int E>
+__device__ __forceinline__ void vec_set(uint4 &x, uint32_t k,
+                                        typename Elem<E>::T v) {
+  const uint32_t w = k * E / 4;
+  uint32_t *p = w == 0 ? &x.x : w == 1 ? &x.y : w == 2 ? &x.z : &x.w;
+  if (E == 8) {
+    const uint64_t v64 = (uint64_t)v;
+    *p = (uint32_t)v64;
+    if (w == 0) x.y = (uint32_t)(v64 >> 32);
+    else x.w = (uint32_t)(v64 >> 32);
+    return;
+  }
+  if (E == 4) {
+    *p = (uint32_t)v;
+    return;
+  }
+  const uint32_t sh = (k * E % 4) * 8;
+  const uint32_t mask = (E == 1 ? 0xffu : 0xffffu) << sh;
+  *p = (*p & ~mask) | (((uint32_t)v << sh) & mask);
+}
+
+// One item: `ntiles` whole tiles, a contiguous range of the job's buffer.
+// Global memory is read and written in 16-byte vectors (the aligned
+// superset of the range; elements outside it are skipped on load and
+// written one by one on store), so a thread keeps 32 bytes in flight
+// whatever the element width; shared memory holds the rows at a padded
+// pitch for the transposed reads.
 template <int E>
 __device__ void batch_item(const BJob &j, const BItem &it, unsigned char *smem) {
   using T = typename Elem<E>::T;
-  const uint32_t rows = it.ntiles * j.a;
-  const uint32_t n = rows * j.row_elems;
-  const uint64_t e0 = it.tile0 * (uint64_t)j.tile_elems;
-  T *buf = reinterpret_cast<T *>(j.base) + e0;
-  // load: contiguous elements -> padded shared rows
-  for (uint32_t base = threadIdx.x; base < n; base += kBatchThreads * 4) {
-    T v[4];
+  constexpr uint32_t VE = 16 / E;  // elements per vector
+  const uint32_t n = it.ntiles * j.a * j.row_elems;
+  T *buf = reinterpret_cast<T *>(j.base) + it.tile0 * (uint64_t)j.tile_elems;
+  const uintptr_t s0 = (uintptr_t)buf;
+  const uintptr_t v0 = s0 & ~(uintptr_t)15;
+  const uint32_t lead = (uint32_t)(s0 - v0) / E;  // elements before the range
+  const uint32_t nv = (lead + n + VE - 1) / VE;
+  const uint4 *vsrc = reinterpret_cast<const uint4 *>(v0);
+  // load: vector v holds elements idx = v*VE - lead + k
+  for (uint32_t base = threadIdx.x; base < nv; base += kBatchThreads * 2) {
+    uint4 x[2];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t idx = base + u * kBatchThreads;
-      if (idx < n) v[u] = __ldcg(buf + idx);
+    for (int u = 0; u < 2; ++u) {
+      const uint32_t v = base + u * kBatchThreads;
+      if (v < nv) x[u] = __ldcg(vsrc + v);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t idx = base + u * kBatchThreads;
-      if (idx < n) {
-        const uint32_t row = fdiv(idx, j.div_row);
-        const uint32_t col = idx - row * j.row_elems;
-        *reinterpret_cast<T *>(smem + row * j.pitch + col * E) = v[u];
+    for (int u = 0; u < 2; ++u) {
+      const uint32_t v = base + u * kBatchThreads;
+      if (v >= nv) continue;
+      int64_t idx = (int64_t)v * VE - lead;
+      const uint32_t k0 = idx < 0 ? (uint32_t)(-idx) : 0u;
+      if (idx < 0) idx = 0;
+      if ((uint64_t)idx >= n) continue;
+      uint32_t row = fdiv((uint32_t)idx, j.div_row);
+      uint32_t col = (uint32_t)idx - row * j.row_elems;
+#pragma unroll
+      for (uint32_t k = 0; k < VE; ++k) {
+        if (k < k0 || (uint64_t)idx >= n) continue;
+        *reinterpret_cast<T *>(smem + row * j.pitch + col * E) =
+            vec_elem<E>(x[u], k);
+        ++idx;
+        if (++col == j.row_elems) {
+          col = 0;
+          ++row;
+        }
       }
     }
   }
   __syncthreads();
-  // store: output o <- (tile t, j, i, sub)
-  for (uint32_t base = threadIdx.x; base < n; base += kBatchThreads * 4) {
-    T v[4];
+  // store: vector v of the output range, output element o <- (tile t,
+  // unit jj of the row, row i, sub-element)
+  uint4 *vdst = reinterpret_cast<uint4 *>(v0);
+  for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads) {
+    int64_t o = (int64_t)v * VE - lead;
+    uint32_t k0 = 0;
+    if (o < 0) {
+      k0 = (uint32_t)(-o);
+      o = 0;
+    }
+    uint32_t unit = (uint32_t)o, sub = 0;
+    if (j.b != 1) {
+      unit = fdiv((uint32_t)o, j.div_b);
+      sub = (uint32_t)o - unit * j.b;
+    }
+    uint32_t t = fdiv(unit, j.div_aB);
+    const uint32_t u2 = unit - t * j.aB;
+    uint32_t jj = fdiv(u2, j.div_a);
+    uint32_t i = u2 - jj * j.a;
+    uint4 x = make_uint4(0, 0, 0, 0);
+    uint32_t kend = VE;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t o = base + u * kBatchThreads;
-      if (o < n) {
-        uint32_t unit = o, sub = 0;
-        if (j.b != 1) {
-          unit = fdiv(o, j.div_b);
-          sub = o - unit * j.b;
+    for (uint32_t k = 0; k < VE; ++k) {
+      if (k < k0) continue;
+      if ((uint64_t)o >= n) {
+        if (kend == VE) kend = k;
+        continue;
+      }
+      vec_set<E>(x, k, *reinterpret_cast<const T *>(
+                           smem + (t * j.a + i) * j.pitch + (jj * j.b + sub) * E));
+      ++o;
+      if (++sub == j.b) {
+        sub = 0;
+        if (++i == j.a) {
+          i = 0;
+          if (++jj == j.B) {
+            jj = 0;
+            ++t;
+          }
         }
-        const uint32_t t = fdiv(unit, j.div_aB);
-        const uint32_t u2 = unit - t * j.aB;
-        const uint32_t jj = fdiv(u2, j.div_a);
-        const uint32_t i = u2 - jj * j.a;
-        v[u] = *reinterpret_cast<const T *>(smem + (t * j.a + i) * j.pitch +
-                                            (jj * j.b + sub) * E);
       }
     }
+    if (k0 == 0 && kend == VE) {
+      __stcg(vdst + v, x);
+    } else {
+      T *d = reinterpret_cast<T *>(v0 + (uintptr_t)v * 16);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t o = base + u * kBatchThreads;
-      if (o < n) __stcg(buf + o, v[u]);
+      for (uint32_t k = 0; k < VE; ++k)
+        if (k >= k0 && k < kend) d[k] = vec_elem<E>(x, k);
     }
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kBatchThreads) k_batch_bs(BatchArgs g) {
+__global__ void __launch_bounds__(kBatchThreads, 2) k_batch_bs(BatchArgs g) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_item;
   while (true) {
@@ -152,15 +250,162 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_bs(BatchArgs g) {
   }
 }
 
-// Warp 0: copies a job descriptor into shared memory (read there by every
-// thread instead of being held in registers).
-__device__ __forceinline__ void copy_job(BJob *dst, const BJob *src) {
-  static_assert(sizeof(BJob) % 4 == 0, "BJob is copied in 32-bit words");
-  const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t k = lane; k < sizeof(BJob) / 4; k += 32)
-    reinterpret_cast<uint32_t *>(dst)[k] =
-        reinterpret_cast<const uint32_t *>(src)[k];
+// Small items (at most kSmallItem bytes), pipelined: the bytes of the next
+// item land in a flat staging buffer by 16-byte cp.async copies (nothing
+// held in registers) while the current item, already scattered into padded
+// rows, is written out.  Shared memory: the flat buffer (g.stage_bytes),
+// then the padded rows.
+template <int E>
+__device__ void small_scatter(const BJob &j, const BItem &it,
+                              const unsigned char *flat, unsigned char *rows) {
+  constexpr uint32_t VE = 16 / E;
+  const uint32_t n = it.ntiles * j.a * j.row_elems;
+  const uintptr_t s0 = (uintptr_t)(j.base + it.tile0 * (uint64_t)j.tile_elems * E);
+  const uint32_t lead = (uint32_t)(s0 & 15) / E;
+  const uint32_t nv = (lead + n + VE - 1) / VE;
+  for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads) {
+    const uint4 x = *reinterpret_cast<const uint4 *>(flat + (size_t)v * 16);
+    int64_t idx = (int64_t)v * VE - lead;
+    const uint32_t k0 = idx < 0 ? (uint32_t)(-idx) : 0u;
+    if (idx < 0) idx = 0;
+    if ((uint64_t)idx >= n) continue;
+    uint32_t row = fdiv((uint32_t)idx, j.div_row);
+    uint32_t col = (uint32_t)idx - row * j.row_elems;
+#pragma unroll
+    for (uint32_t k = 0; k < VE; ++k) {
+      if (k < k0 || (uint64_t)idx >= n) continue;
+      *reinterpret_cast<typename Elem<E>::T *>(rows + row * j.pitch + col * E) =
+          vec_elem<E>(x, k);
+      ++idx;
+      if (++col == j.row_elems) {
+        col = 0;
+        ++row;
+      }
+    }
+  }
 }
+
+template <int E>
+__device__ void small_store(const BJob &j, const BItem &it,
+                            const unsigned char *rows) {
+  using T = typename Elem<E>::T;
+  constexpr uint32_t VE = 16 / E;
+  const uint32_t n = it.ntiles * j.a * j.row_elems;
+  const uintptr_t s0 = (uintptr_t)(j.base + it.tile0 * (uint64_t)j.tile_elems * E);
+  const uintptr_t v0 = s0 & ~(uintptr_t)15;
+  const uint32_t lead = (uint32_t)(s0 - v0) / E;
+  const uint32_t nv = (lead + n + VE - 1) / VE;
+  uint4 *vdst = reinterpret_cast<uint4 *>(v0);
+  for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads) {
+    int64_t o = (int64_t)v * VE - lead;
+    const uint32_t k0 = o < 0 ? (uint32_t)(-o) : 0u;
+    if (o < 0) o = 0;
+    uint32_t unit = (uint32_t)o, sub = 0;
+    if (j.b != 1) {
+      unit = fdiv((uint32_t)o, j.div_b);
+      sub = (uint32_t)o - unit * j.b;
+    }
+    uint32_t t = fdiv(unit, j.div_aB);
+    const uint32_t u2 = unit - t * j.aB;
+    uint32_t jj = fdiv(u2, j.div_a);
+    uint32_t i = u2 - jj * j.a;
+    uint4 x = make_uint4(0, 0, 0, 0);
+    uint32_t kend = VE;
+#pragma unroll
+    for (uint32_t k = 0; k < VE; ++k) {
+      if (k < k0) continue;
+      if ((uint64_t)o >= n) {
+        if (kend == VE) kend = k;
+        continue;
+      }
+      vec_set<E>(x, k, *reinterpret_cast<const T *>(
+                           rows + (t * j.a + i) * j.pitch + (jj * j.b + sub) * E));
+      ++o;
+      if (++sub == j.b) {
+        sub = 0;
+        if (++i == j.a) {
+          i = 0;
+          if (++jj == j.B) {
+            jj = 0;
+            ++t;
+          }
+        }
+      }
+    }
+    if (k0 == 0 && kend == VE) {
+      __stcg(vdst + v, x);
+    } else {
+      T *d = reinterpret_cast<T *>(v0 + (uintptr_t)v * 16);
+#pragma unroll
+      for (uint32_t k = 0; k < VE; ++k)
+        if (k >= k0 && k < kend) d[k] = vec_elem<E>(x, k);
+    }
+  }
+}
+
+// All threads: 16-byte cp.async copies of the item's aligned superset into
+// the flat buffer, one commit group.
+__device__ __forceinline__ void small_issue(const BJob &j, const BItem &it,
+                                            unsigned char *flat) {
+  const uint64_t nbytes = (uint64_t)it.ntiles * j.tile_elems * j.e;
+  const uintptr_t s0 = (uintptr_t)(j.base + it.tile0 * (uint64_t)j.tile_elems * j.e);
+  const uintptr_t v0 = s0 & ~(uintptr_t)15;
+  const uint32_t nv = (uint32_t)((s0 - v0 + nbytes + 15) / 16);
+  for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads)
+    cp_async16(flat + (size_t)v * 16, (const void *)(v0 + (uintptr_t)v * 16));
+  cp_async_commit();
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 2) k_batch_small(BatchArgs g) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *flat = smem;
+  unsigned char *rows = smem + g.stage_bytes;
+  __shared__ uint32_t s_item;
+  __shared__ __align__(16) BJob s_jobs[2];
+  __shared__ __align__(16) BItem s_items[2];
+  const uint32_t warp = threadIdx.x >> 5;
+  // claim an item into slot `sl` (job and item copied to shared memory);
+  // returns false when the work is done
+  auto claim = [&](int sl) -> bool {
+    if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);
+    __syncthreads();
+    const uint32_t k = s_item;
+    if (k < g.nitems && warp == 0) {
+      const BItem it = g.items[k];
+      copy_job(&s_jobs[sl], &g.jobs[it.job]);
+      if ((threadIdx.x & 31) == 0) s_items[sl] = it;
+    }
+    __syncthreads();
+    return k < g.nitems;
+  };
+  if (!claim(0)) return;
+  small_issue(s_jobs[0], s_items[0], flat);
+  for (uint32_t n = 0;; ++n) {
+    const int st = n & 1, nx = st ^ 1;
+    cp_async_wait_all();
+    __syncthreads();  // the flat buffer holds item n
+    const BJob &j = s_jobs[st];
+    switch (j.e) {
+      case 1: small_scatter<1>(j, s_items[st], flat, rows); break;
+      case 2: small_scatter<2>(j, s_items[st], flat, rows); break;
+      case 4: small_scatter<4>(j, s_items[st], flat, rows); break;
+      default: small_scatter<8>(j, s_items[st], flat, rows); break;
+    }
+    // (claim's first barrier also orders the scatter before the next
+    // item's copies overwrite the flat buffer)
+    const bool more = claim(nx);
+    if (more) small_issue(s_jobs[nx], s_items[nx], flat);
+    switch (j.e) {
+      case 1: small_store<1>(j, s_items[st], rows); break;
+      case 2: small_store<2>(j, s_items[st], rows); break;
+      case 4: small_store<4>(j, s_items[st], rows); break;
+      default: small_store<8>(j, s_items[st], rows); break;
+    }
+    __syncthreads();  // the padded rows are free
+    if (!more) break;
+  }
+}
+
 
 // Writes nrows x ncols staged elements (b == 1) transposed: output row jj
 // (stride `ostride` elements from `dst`) gets staged column jj.  A warp
@@ -751,6 +996,7 @@ struct lm_batch_st {
   int nwaves = 0;
   char *d_arena = nullptr;  // scratch of the staged jobs of one wave
   uint64_t cap_arena = 0, need_arena = 0;
+  uint64_t arena_limit = 0;  // lm_batch_set_arena; 0: LM_BATCH_SCRATCH_MB
   std::vector<uint32_t> large;  // indices of jobs run by the planner
   std::vector<lm::Normalized> norm;
   // device side
@@ -938,7 +1184,9 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
   bt->nwaves = 0;
   bt->need_arena = 0;
   uint64_t wave_used = 0;
-  const uint64_t arena_cap = (flags & LM_BATCH_NO_SCRATCH) ? 0 : arena_bytes();
+  const uint64_t arena_cap = (flags & LM_BATCH_NO_SCRATCH) ? 0
+                             : bt->arena_limit    ? bt->arena_limit
+                                                  : arena_bytes();
   bt->norm.assign(n, Normalized());
   memset(&bt->stats, 0, sizeof(bt->stats));
   for (int k = 0; k < n; ++k) {
@@ -1028,6 +1276,12 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
         bt->stats.big_bytes += bytes;
         continue;
       }
+      // a large 100 that the stash plan serves (3 x payload instead of the
+      // staged form's 4) goes to the planner
+      if (nz.T == 1 && unit < 128 && bytes >= kStashPreferBytes &&
+          nz.a >= 16ull * (uint64_t)di.sms && nz.a * nz.B >= (1ull << 20) &&
+          plan_stash(nz.a, nz.B, (uint32_t)nz.b, jb.elem_bytes).feasible)
+        goto planner;
       // staged: the job fits the arena (in the current wave or a new one)
       if (stageable) {
         if (bt->nwaves == 0 || wave_used + foot > arena_cap) {
@@ -1248,6 +1502,36 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
 
 }  // namespace lm
 
+static bool launch_small(cudaStream_t s, const BJob *d_jobs,
+                         const BItem *d_items, uint32_t nitems,
+                         uint32_t *counter) {
+  if (nitems == 0) return false;
+  // flat buffer: an item's bytes with its 16-byte superset; padded rows
+  constexpr size_t kFlat = (kSmallItem + 32 + 127) / 128 * 128;
+  const size_t smem = kFlat + kSmallItem + 256;
+  const DeviceInfo &di = device_info();
+  cudaError_t err = cudaFuncSetAttribute(
+      k_batch_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return set_error("batch: smem attribute");
+  int occ = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_small,
+                                                      kBatchThreads, smem);
+  if (err != cudaSuccess || occ < 1) return set_error("batch: occupancy");
+  const uint32_t grid =
+      (uint32_t)std::min<uint64_t>((uint64_t)di.sms * occ, nitems);
+  BatchArgs g{};
+  g.jobs = d_jobs;
+  g.items = d_items;
+  g.nitems = nitems;
+  g.counter = counter;
+  g.status = nullptr;
+  g.stage_bytes = (uint32_t)kFlat;
+  ProfScope ps(s, "batch_tiles");
+  k_batch_small<<<grid, kBatchThreads, smem, s>>>(g);
+  if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
+  return false;
+}
+
 static bool launch_items(cudaStream_t s, const BJob *d_jobs,
                          const BItem *d_items, uint32_t nitems,
                          uint32_t *counter, size_t smem) {
@@ -1453,8 +1737,8 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   }
   if (!bt->small.empty() || !bt->big.empty()) {
     const cudaStream_t ts = next_stream();
-    if (launch_items(ts, bt->d_jobs, bt->d_items, (uint32_t)bt->small.size(),
-                     bt->d_counters, kSmallItem + 256))
+    if (launch_small(ts, bt->d_jobs, bt->d_items, (uint32_t)bt->small.size(),
+                     bt->d_counters))
       return true;
     if (!bt->big.empty()) {
       const DeviceInfo &di = device_info();
@@ -1565,6 +1849,12 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
   }
   if (plan_batch(bt, jobs, njobs, flags)) return true;
   return enqueue_batch(bt, s, jobs, flags, nullptr);
+}
+
+bool lm_batch_set_arena(lm_batch_t bt, unsigned long long bytes) {
+  if (!bt) return set_error("batch: null handle");
+  bt->arena_limit = bytes;
+  return false;
 }
 
 bool lm_batch_stats_get(lm_batch_t bt, lm_batch_stats *out) {

@@ -144,6 +144,15 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
                : "memory");
 }
 
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// Waits for all of this thread's committed cp.async groups.
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // Arrives on `bar` once all of this thread's earlier cp.async copies have
 // completed (the barrier's expected count must include this arrival).
 __device__ __forceinline__ void cp_async_mbar_arrive_noinc(uint64_t *bar) {

@@ -9,9 +9,9 @@
 //    not fit waits, and so do the ones behind it).  Requests whose data is on
 //    the host are staged through a device pool of the budget's size;
 //  * lanes: requests are sorted by payload into three lanes (small, medium,
-//    large), each with its own stream (small ones at the highest priority),
-//    its own lm_batch_t and up to kSlots batches in flight, so a long
-//    conversion does not hold back short ones;
+//    large) with up to kSlots batches in flight each; every slot has its own
+//    stream (small lanes at the highest priority) and lm_batch_t, so a long
+//    conversion does not hold back short ones and batches overlap;
 //  * batching: when a lane has a free slot, every admitted request queued on
 //    it (up to the lane's batch limits) becomes one lm_batch_run;
 //  * completion: a host function enqueued after each batch stamps the time
@@ -47,9 +47,11 @@ constexpr int kLanes = 3;
 constexpr int kSlots = 2;
 // lane by payload: <= 2 MiB, <= 64 MiB, larger
 constexpr uint64_t kLaneLimit[kLanes - 1] = {2ull << 20, 64ull << 20};
-// batch limits per lane: requests and payload bytes
+// batch limits per lane: requests and payload bytes; staging arena of each
+// slot's batch handle
 constexpr size_t kLaneMaxReqs[kLanes] = {4096, 256, 8};
 constexpr uint64_t kLaneMaxBytes[kLanes] = {1ull << 30, 4ull << 30, 8ull << 30};
+constexpr uint64_t kLaneArena[kLanes] = {1ull << 30, 2ull << 30, 4ull << 30};
 
 struct SReq {
   uint64_t ticket = 0;
@@ -63,6 +65,8 @@ struct SReq {
 };
 
 struct Slot {
+  cudaStream_t stream = nullptr;  // batches of different slots overlap
+  lm_batch_t batch = nullptr;
   std::vector<SReq> reqs;
   std::vector<lm_job> jobs;
   std::atomic<int> done{0};
@@ -73,8 +77,6 @@ struct Slot {
 };
 
 struct Lane {
-  cudaStream_t stream = nullptr;
-  lm_batch_t batch = nullptr;
   std::deque<SReq> queue;  // admitted, waiting for a slot
   Slot slots[kSlots];
 };
@@ -176,12 +178,13 @@ void lm_serve_st::launch(Lane &ln, Slot &sl) {
     if (q.host) {
       q.job.buf = pool + q.pool_off;
       cudaMemcpyAsync(q.job.buf, q.r.src, q.bytes, cudaMemcpyHostToDevice,
-                      ln.stream);
+                      sl.stream);
     }
     sl.jobs.push_back(q.job);
   }
-  sl.status = lm_batch_run(ln.batch, ln.stream, sl.jobs.data(),
-                           (int)sl.jobs.size(), 0)
+  // no autotuning here: timing candidate plans would stall this thread
+  sl.status = lm_batch_run(sl.batch, sl.stream, sl.jobs.data(),
+                           (int)sl.jobs.size(), LM_BATCH_NO_TUNE)
                   ? 1
                   : 0;
   if (sl.status) {
@@ -191,13 +194,13 @@ void lm_serve_st::launch(Lane &ln, Slot &sl) {
   for (SReq &q : sl.reqs)
     if (q.host)
       cudaMemcpyAsync(q.r.dst, q.job.buf, q.bytes, cudaMemcpyDeviceToHost,
-                      ln.stream);
+                      sl.stream);
   sl.done.store(0);
   sl.busy = true;
   sl.wake = &cv;
-  if (cudaLaunchHostFunc(ln.stream, slot_done, &sl) != cudaSuccess) {
+  if (cudaLaunchHostFunc(sl.stream, slot_done, &sl) != cudaSuccess) {
     // no callback: wait here so the slot still completes
-    cudaStreamSynchronize(ln.stream);
+    cudaStreamSynchronize(sl.stream);
     slot_done(&sl);
   }
 }
@@ -321,19 +324,26 @@ bool lm_serve_create(lm_serve_t *out, unsigned long long budget_bytes) {
   s->budget = budget_bytes;
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);  // hi: numerically lowest
-  for (int li = 0; li < kLanes; ++li) {
-    Lane &ln = s->lanes[li];
+  bool ok = true;
+  for (int li = 0; li < kLanes && ok; ++li) {
     const int prio = li == 0 ? hi : (li == 1 ? (lo + hi) / 2 : lo);
-    if (cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, prio) !=
-            cudaSuccess ||
-        lm_batch_create(&ln.batch)) {
-      for (int k = 0; k <= li; ++k) {
-        if (s->lanes[k].stream) cudaStreamDestroy(s->lanes[k].stream);
-        if (s->lanes[k].batch) lm_batch_destroy(s->lanes[k].batch);
-      }
-      delete s;
-      return lm::set_error("serve: cannot create the lane streams");
+    for (Slot &sl : s->lanes[li].slots) {
+      ok = ok &&
+           cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking,
+                                        prio) == cudaSuccess &&
+           !lm_batch_create(&sl.batch) &&
+           !lm_batch_set_arena(sl.batch, kLaneArena[li]);
+      if (!ok) break;
     }
+  }
+  if (!ok) {
+    for (Lane &ln : s->lanes)
+      for (Slot &sl : ln.slots) {
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.batch) lm_batch_destroy(sl.batch);
+      }
+    delete s;
+    return lm::set_error("serve: cannot create the lane streams");
   }
   s->worker = std::thread([s] { s->run(); });
   *out = s;
@@ -533,11 +543,12 @@ void lm_serve_destroy(lm_serve_t s) {
   }
   s->cv.notify_one();
   if (s->worker.joinable()) s->worker.join();
-  for (Lane &ln : s->lanes) {
-    if (ln.stream) cudaStreamSynchronize(ln.stream);
-    if (ln.batch) lm_batch_destroy(ln.batch);
-    if (ln.stream) cudaStreamDestroy(ln.stream);
-  }
+  for (Lane &ln : s->lanes)
+    for (Slot &sl : ln.slots) {
+      if (sl.stream) cudaStreamSynchronize(sl.stream);
+      if (sl.batch) lm_batch_destroy(sl.batch);
+      if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
   if (s->pool) cudaFree(s->pool);
   delete s;
 }

@@ -56,6 +56,7 @@ _SIGS = {
     "lm_batch_destroy": (None, [_VP]),
     "lm_batch_run": (_B, [_VP, _VP, _VP, _I, ctypes.c_uint]),
     "lm_batch_stats_get": (_B, [_VP, _VP]),
+    "lm_batch_set_arena": (_B, [_VP, ctypes.c_ulonglong]),
     "lm_tune_entries": (_I, []),
     "lm_serve_create": (_B, [_VP, ctypes.c_ulonglong]),
     "lm_serve_submit": (_B, [_VP, _VP, _ULLP]),
