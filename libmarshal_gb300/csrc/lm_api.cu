@@ -336,8 +336,10 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   // any shape through scratch: block transposes out of place, then a copy
   // back (4 x payload, but every access in whole sectors); falls through
   // when the scratch cannot be had
+  // (units of 128 bytes and more move as whole lines in cycle following,
+  // which needs no scratch and is as fast)
   if (m == Method::Staged ||
-      (m == Method::Auto && T * a * B * b * e >= (1ull << 20) &&
+      (m == Method::Auto && U < 128 && T * a * B * b * e >= (1ull << 20) &&
        !getenv("LM_NO_STAGED"))) {
     if (staged0100_applies(T, a, B, b, e)) {
       Scratch sc;
