@@ -570,48 +570,57 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
   const uint64_t U = (uint64_t)b * e;
   const DeviceInfo &di = device_info();
   const uint64_t max_smem = (uint64_t)di.max_smem_optin - 1024;
-  // aim for 512-byte strips; shrink the strip when the chunk would not fit.
-  // LM_STASH_STRIP / LM_STASH_PER_SM override the choice (tuning sweeps).
+  // Strip per step: the largest (1024 bytes down to 128, in steps of 128)
+  // that keeps a CTA's step at most kStepBytes and three ring stages within
+  // shared memory, two CTAs per SM first.  Longer steps amortise each step's
+  // handshakes; the sweep on both headline directions and fp64 peaked near
+  // 32-40 KB per step.  LM_STASH_STRIP / LM_STASH_PER_SM force a choice.
   const char *es = getenv("LM_STASH_STRIP");
   const char *ep = getenv("LM_STASH_PER_SM");
-  const uint64_t strips_default[3] = {512ull, 256ull, 128ull};
-  uint64_t strips[3] = {strips_default[0], strips_default[1], strips_default[2]};
-  if (es && atoll(es) > 0) strips[0] = strips[1] = strips[2] = (uint64_t)atoll(es);
-  const int per_sms[2] = {ep && atoi(ep) == 1 ? 1 : 2, 1};
   const char *em = getenv("LM_STASH_MARGIN");
   const uint32_t margin =
       em && atoi(em) > 0 && atoi(em) < 64 ? (uint32_t)atoi(em) : kStashMargin;
-  for (uint64_t strip : strips) {
+  const int per_sms[2] = {ep && atoi(ep) == 1 ? 1 : 2, 1};
+  constexpr uint64_t kStepBytes = 40 * 1024;
+  auto try_plan = [&](uint64_t strip, int per_sm) -> bool {
+    const uint64_t ctas = (uint64_t)di.sms * per_sm;
+    const uint64_t W = (A + ctas - 1) / ctas;
     uint64_t g = std::max<uint64_t>(1, strip / U);
     if (g > B) g = B;
     const uint64_t G = (B + g - 1) / g;
     const uint32_t pitch = stash_pitch(g * U, e);
-    for (int per_sm : per_sms) {
-      const uint64_t ctas = (uint64_t)di.sms * per_sm;
-      const uint64_t W = (A + ctas - 1) / ctas;
-      const uint64_t smem = (uint64_t)kStages * stash_stage_bytes(W, pitch);
-      if (smem > max_smem / per_sm) continue;
-      if (W * g * b >= 0xffffffffull || g * b >= 0xffffffffull) continue;
-      if (G > 65535) continue;  // K1 puts groups on grid.y
-      if (W > 32u * kMaxRowBlocks) continue;
-      if ((A + W - 1) / W > kMaxChunks) continue;
-      const uint64_t nch = (A + W - 1) / W;
-      if ((uint64_t)wave_occupancy_e(e, (size_t)smem) * di.sms < nch) continue;
-      p.feasible = true;
-      p.g = (uint32_t)g;
-      p.G = (uint32_t)G;
-      p.W = (uint32_t)W;
-      p.nchunks = (uint32_t)((A + W - 1) / W);
-      p.pitch = pitch;
-      p.smem_bytes = (size_t)smem;
-      p.ctas_per_sm = per_sm;
-      p.margin = margin;
-      p.A = A;
-      uint64_t total = 0;
-      for (uint64_t i = 0; i < A; ++i)
-        total += stash_slot_bytes(i, g, A, B, G, U, margin);
-      p.stash_bytes = (size_t)total;
-      return p;
+    const uint64_t smem = (uint64_t)kStages * stash_stage_bytes(W, pitch);
+    const uint64_t nch = (A + W - 1) / W;
+    if (smem > max_smem / per_sm || W * g * b >= 0xffffffffull ||
+        g * b >= 0xffffffffull || G > 65535 || W > 32u * kMaxRowBlocks ||
+        nch > kMaxChunks ||
+        (uint64_t)wave_occupancy_e(e, (size_t)smem) * di.sms < nch)
+      return false;
+    p.feasible = true;
+    p.g = (uint32_t)g;
+    p.G = (uint32_t)G;
+    p.W = (uint32_t)W;
+    p.nchunks = (uint32_t)nch;
+    p.pitch = pitch;
+    p.smem_bytes = (size_t)smem;
+    p.ctas_per_sm = per_sm;
+    p.margin = margin;
+    p.A = A;
+    uint64_t total = 0;
+    for (uint64_t i = 0; i < A; ++i)
+      total += stash_slot_bytes(i, g, A, B, G, U, margin);
+    p.stash_bytes = (size_t)total;
+    return true;
+  };
+  for (int per_sm : per_sms) {
+    if (es && atoll(es) > 0) {
+      if (try_plan((uint64_t)atoll(es), per_sm)) return p;
+      continue;
+    }
+    const uint64_t W = (A + (uint64_t)di.sms * per_sm - 1) / ((uint64_t)di.sms * per_sm);
+    for (uint64_t strip = 1024; strip >= 128; strip -= 128) {
+      if (W * strip > kStepBytes && strip > 128) continue;
+      if (try_plan(strip, per_sm)) return p;
     }
   }
   return p;
