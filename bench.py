@@ -124,15 +124,20 @@ class ClockSampler:
 
 # ---- distributed -------------------------------------------------------------
 
-def dist_setup(n):
+def dist_setup(n, backend=None):
+    """Replicas: one process per GPU (torchrun's RANK / LOCAL_RANK /
+    WORLD_SIZE), NCCL between GPUs; backend="gloo" runs the same
+    coordination on CPU (tests)."""
     import torch
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
     if ws > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     elif torch.cuda.is_available():
         torch.cuda.set_device(0)
     return ws, rank, local
@@ -149,9 +154,16 @@ def max_over_ranks(ws, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_rate(ws, bytes_per_rank_step, steps, max_ms):
+    """Whole-job GB/s of replicas: every rank's bytes over the slowest
+    rank's time."""
+    return ws * bytes_per_rank_step * steps / (max_ms / 1e3) / 1e9
 
 
 # ---- CPU baseline (the reference's CPU path, restated in the oracle) ---------
@@ -295,7 +307,7 @@ def run_ours(args, ws, rank, local):
     verified = bool(torch.equal(buf, orig))
     del orig
 
-    value = ws * 2.0 * PAYLOAD * args.steps / (ms / 1e3) / 1e9
+    value = aggregate_rate(ws, 2.0 * PAYLOAD, args.steps, ms)
     peak, peak_kind = peak_hbm()
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
     roof = None

@@ -101,3 +101,40 @@ def test_python_api_host_logic():
         TransposeArrayInPlace(torch.zeros(2, 3, 4))
     with pytest.raises(TypeError):
         TransposeArrayInPlace(torch.zeros(10, 9), a=3, b=1)
+
+
+def test_cl_compat_header_compiles_and_links(built, tmp_path):
+    """A C program written against the reference's cl_* names builds with
+    include/cl_marshal_compat.h and links against the library; it only
+    exercises argument checks (no device needed)."""
+    import shutil
+    import subprocess
+    from libmarshal_gb300 import lm
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "uses_cl.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "cl_marshal_compat.h"
+int main(void) {
+  cl_ulong et = 0;
+  /* element size and divisibility are checked before any device work */
+  int e1 = cl_aos_asta_bs(NULL, NULL, 10, 3, 4);           /* 10 % 4 != 0 */
+  int e2 = cl_transpose_100(NULL, (cl_mem)0x1002, 4, 5, 1, NULL); /* misaligned */
+  (void)et;
+  printf("%d %d %s\n", e1, e2, lm_last_error());
+  cl_marshal_finalize();
+  return (e1 && e2) ? 0 : 1;
+}
+""")
+    exe = tmp_path / "uses_cl"
+    libdir = os.path.dirname(lm.LIB_PATH)
+    subprocess.check_call([cc, "-std=c99", str(src), "-I",
+                           os.path.join(root, "include"), "-L", libdir,
+                           "-llmarshal", "-Wl,-rpath," + libdir, "-o",
+                           str(exe)])
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "aligned" in out.stdout
