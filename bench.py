@@ -759,12 +759,18 @@ def run_serve_workload(args, ws, rank, local):
             off += size
         row = {"rate_per_s": rate, "requests": len(reqs),
                "payload_bytes": payload}
+        nw = min(len(reqs), 200)  # warm-up: the trace's first requests, at once
         for mode in ("served", "plain"):
             torch.cuda.synchronize()
             srv = None if mode == "plain" else lm.Server(budget)
+            lm.serve_replay(srv, reqs[:nw], [0] * nw, None,
+                            plain=(mode == "plain"))
+            st0 = srv.stats() if srv is not None else None
             res = lm.serve_replay(srv, reqs, arrival, after,
                                   plain=(mode == "plain"))
             st = srv.stats() if srv is not None else None
+            if st is not None:
+                st["batches"] -= st0["batches"]
             if srv is not None:
                 srv.close()
             if any(r[0] for r in res):
@@ -797,7 +803,9 @@ def run_serve_workload(args, ws, rank, local):
         "config": {"workload": "serve_poisson_4KiB_512MiB",
                    "budget_bytes": budget, "ring_bytes": ring,
                    "requests_per_rate": args.serve_n,
-                   "rates_per_s": list(args.serve_rates)},
+                   "rates_per_s": list(args.serve_rates),
+                   "warmup": "the trace's first 200 requests, untimed, "
+                             "before each timed replay"},
         "p50_ms": top["served"]["p50_ms"], "p99_ms": top["served"]["p99_ms"],
         "peak": peak, "peak_kind": peak_kind, "rates": results,
     }

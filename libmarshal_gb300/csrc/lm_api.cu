@@ -79,7 +79,7 @@ static bool cuda_fail(cudaError_t e, const char *what) {
 
 // ---- scratch ----------------------------------------------------------------
 
-static void pool_keep_memory() {
+void pool_keep_memory() {
   static bool done[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);

@@ -997,6 +997,9 @@ struct lm_batch_st {
   char *d_arena = nullptr;  // scratch of the staged jobs of one wave
   uint64_t cap_arena = 0, need_arena = 0;
   uint64_t arena_limit = 0;  // lm_batch_set_arena; 0: LM_BATCH_SCRATCH_MB
+  cudaStream_t last_stream = nullptr;  // stream of the previous run
+  bool used = false;
+  std::vector<void *> retired_pinned;  // grown-out staging buffers
   std::vector<uint32_t> large;  // indices of jobs run by the planner
   std::vector<lm::Normalized> norm;
   // device side
@@ -1041,46 +1044,59 @@ static void drop_graph(lm_batch_t bt) {
   bt->gkey = 0;
 }
 
-static bool grow(lm_batch_t bt, size_t njobs, size_t nitems) {
+// Grows the device tables, the arena and the pinned staging buffer.  Device
+// memory comes from the stream-ordered pool and is released on the stream of
+// the run that last used it: no device-wide synchronisation (a plain
+// cudaFree would wait for all work, stalling a server).  Retired pinned
+// buffers are kept until the handle is destroyed for the same reason.
+static bool grow(lm_batch_t bt, cudaStream_t s, size_t njobs, size_t nitems) {
+  const cudaStream_t fs = bt->used ? bt->last_stream : s;
+  pool_keep_memory();
+  auto regrow = [&](void **p, size_t bytes) -> bool {
+    // inside a capture the pool calls would become graph-owned memory
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess ||
+        cap != cudaStreamCaptureStatusNone)
+      return false;
+    if (*p) cudaFreeAsync(*p, fs);
+    *p = nullptr;
+    if (cudaMallocAsync(p, bytes, s) != cudaSuccess) {
+      cudaGetLastError();
+      *p = nullptr;
+      return false;
+    }
+    return true;
+  };
   if (bt->need_arena > bt->cap_arena) {
     drop_graph(bt);
-    if (bt->d_arena) cudaFree(bt->d_arena);
-    bt->d_arena = nullptr;
     bt->cap_arena = 0;
-    if (cudaMalloc(&bt->d_arena, bt->need_arena) != cudaSuccess) {
-      bt->d_arena = nullptr;
+    if (!regrow(reinterpret_cast<void **>(&bt->d_arena), bt->need_arena))
       return set_error("batch: cannot allocate the staging arena");
-    }
     bt->cap_arena = bt->need_arena;
   }
   if (njobs > bt->cap_jobs) {
     drop_graph(bt);
-    if (bt->d_jobs) cudaFree(bt->d_jobs);
-    bt->cap_jobs = std::max<size_t>(njobs, 2 * bt->cap_jobs);
-    if (cudaMalloc(&bt->d_jobs, bt->cap_jobs * sizeof(BJob)) != cudaSuccess) {
-      bt->d_jobs = nullptr;
-      bt->cap_jobs = 0;
+    const size_t cap = std::max<size_t>(njobs, 2 * bt->cap_jobs);
+    bt->cap_jobs = 0;
+    if (!regrow(reinterpret_cast<void **>(&bt->d_jobs), cap * sizeof(BJob)))
       return set_error("batch: cannot allocate the job table");
-    }
+    bt->cap_jobs = cap;
   }
   if (nitems > bt->cap_items) {
     drop_graph(bt);
-    if (bt->d_items) cudaFree(bt->d_items);
-    bt->cap_items = std::max<size_t>(nitems, 2 * bt->cap_items);
-    if (cudaMalloc(&bt->d_items, bt->cap_items * sizeof(BItem)) != cudaSuccess) {
-      bt->d_items = nullptr;
-      bt->cap_items = 0;
+    const size_t cap = std::max<size_t>(nitems, 2 * bt->cap_items);
+    bt->cap_items = 0;
+    if (!regrow(reinterpret_cast<void **>(&bt->d_items), cap * sizeof(BItem)))
       return set_error("batch: cannot allocate the item list");
-    }
+    bt->cap_items = cap;
   }
-  if (!bt->d_counters) {
-    if (cudaMalloc(&bt->d_counters, kCounterBytes) != cudaSuccess)
-      return set_error("batch: cannot allocate counters");
-  }
+  if (!bt->d_counters &&
+      !regrow(reinterpret_cast<void **>(&bt->d_counters), kCounterBytes))
+    return set_error("batch: cannot allocate counters");
   const size_t stage = njobs * sizeof(BJob) + nitems * sizeof(BItem) + 256;
   if (stage > bt->cap_stage) {
-    if (bt->uploaded) cudaEventSynchronize(bt->uploaded);
-    if (bt->h_stage) cudaFreeHost(bt->h_stage);
+    if (bt->h_stage) bt->retired_pinned.push_back(bt->h_stage);
+    bt->h_stage = nullptr;
     bt->cap_stage = std::max(stage, 2 * bt->cap_stage);
     if (cudaMallocHost(&bt->h_stage, bt->cap_stage) != cudaSuccess) {
       bt->h_stage = nullptr;
@@ -1635,7 +1651,8 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
                           unsigned flags, char *stage) {
   const size_t nj = bt->jobs.size();
   const size_t ni = item_count(bt);
-  if (grow(bt, std::max<size_t>(nj, 1), std::max<size_t>(ni, 1))) return true;
+  if (grow(bt, s, std::max<size_t>(nj, 1), std::max<size_t>(ni, 1)))
+    return true;
   // the large jobs need no table: they start first, on the side streams
   unsigned used = 0;
   if (enqueue_large(bt, s, jobs, flags, &used)) return true;
@@ -1678,6 +1695,8 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
             cudaSuccess)
       return set_error("batch: upload event");
     cudaEventRecord(bt->uploaded, s);
+    bt->last_stream = s;
+    bt->used = true;
   }
   if (cudaMemsetAsync(bt->d_counters, 0, kCounterBytes, s) != cudaSuccess)
     return set_error("batch: counter clear");
@@ -1773,9 +1792,10 @@ void lm_batch_destroy(lm_batch_t bt) {
   if (bt->d_jobs) cudaFree(bt->d_jobs);
   if (bt->d_items) cudaFree(bt->d_items);
   if (bt->d_counters) cudaFree(bt->d_counters);
-  if (bt->d_arena) cudaFree(bt->d_arena);
+  if (bt->d_arena) cudaFree(bt->d_arena);  // waits for its users
   if (bt->h_stage) cudaFreeHost(bt->h_stage);
   if (bt->h_gstage) cudaFreeHost(bt->h_gstage);
+  for (void *p : bt->retired_pinned) cudaFreeHost(p);
   if (bt->uploaded) cudaEventDestroy(bt->uploaded);
   for (int k = 0; k < lm::kSideStreams; ++k) {
     if (bt->side[k]) cudaStreamDestroy(bt->side[k]);
@@ -1796,6 +1816,8 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
     if (bt->gexec && key == bt->gkey) {
       if (cudaGraphLaunch(bt->gexec, s) != cudaSuccess)
         return set_error("batch: graph launch");
+      bt->last_stream = s;
+      bt->used = true;
       return false;
     }
     if (key == bt->seen_key) {
@@ -1803,7 +1825,7 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
       // initialised by the first run, outside any capture, and the tuned
       // plans are cached), then replay
       if (plan_batch(bt, jobs, njobs, flags)) return true;
-      if (grow(bt, std::max<size_t>(bt->jobs.size(), 1),
+      if (grow(bt, s, std::max<size_t>(bt->jobs.size(), 1),
                std::max<size_t>(item_count(bt), 1)))
         return true;
       if (bt->gexec) {
@@ -1843,6 +1865,8 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
       bt->gkey = key;
       if (cudaGraphLaunch(bt->gexec, s) != cudaSuccess)
         return set_error("batch: graph launch");
+      bt->last_stream = s;
+      bt->used = true;
       return false;
     }
     bt->seen_key = key;

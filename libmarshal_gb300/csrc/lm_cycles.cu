@@ -261,19 +261,21 @@ static cudaError_t leaders_for(cudaStream_t s, uint32_t a, uint32_t B,
     return into_scratch();
   CycEntry en;
   en.bytes = bytes;
-  cudaError_t err = cudaMalloc(&en.mem, bytes);
+  // stream-ordered: a plain cudaMalloc may synchronise the device
+  pool_keep_memory();
+  cudaError_t err = cudaMallocAsync(&en.mem, bytes, s);
   if (err != cudaSuccess) {
     cudaGetLastError();  // clear the failed allocation's error
     return into_scratch();
   }
   if ((err = cudaEventCreateWithFlags(&en.ready, cudaEventDisableTiming)) !=
       cudaSuccess) {
-    cudaFree(en.mem);
+    cudaFreeAsync(en.mem, s);
     return err;
   }
   if ((err = run_leaders(s, a, m, L, w32, en.mem)) != cudaSuccess ||
       (err = cudaEventRecord(en.ready, s)) != cudaSuccess) {
-    cudaFree(en.mem);
+    cudaFreeAsync(en.mem, s);
     cudaEventDestroy(en.ready);
     return err;
   }

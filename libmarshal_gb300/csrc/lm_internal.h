@@ -139,6 +139,10 @@ bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
 bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
                       uint64_t a, uint64_t B, uint64_t b, int tune);
 
+// Keeps the current device's stream-ordered pool from returning freed
+// blocks to the system (scratch and arenas are reused call after call).
+void pool_keep_memory();
+
 // Per-device persistent status word that waiting kernels OR their failures
 // into (allocated on first use); lm_api.cu reads and clears it.
 uint32_t *device_status_word();

@@ -690,21 +690,23 @@ static cudaError_t stash_offsets(cudaStream_t s, StashArgs &g) {
     return launch_offsets(s, g);
   RoffEntry en;
   en.bytes = bytes;
-  cudaError_t err = cudaMalloc(&en.mem, bytes);
+  // stream-ordered: a plain cudaMalloc may synchronise the device
+  pool_keep_memory();
+  cudaError_t err = cudaMallocAsync(&en.mem, bytes, s);
   if (err != cudaSuccess) {
     cudaGetLastError();  // clear the failed allocation's error
     return launch_offsets(s, g);  // into scratch
   }
   if ((err = cudaEventCreateWithFlags(&en.ready, cudaEventDisableTiming)) !=
       cudaSuccess) {
-    cudaFree(en.mem);
+    cudaFreeAsync(en.mem, s);
     return err;
   }
   StashArgs gc = g;
   gc.roff = reinterpret_cast<const uint64_t *>(en.mem);
   if ((err = launch_offsets(s, gc)) != cudaSuccess ||
       (err = cudaEventRecord(en.ready, s)) != cudaSuccess) {
-    cudaFree(en.mem);
+    cudaFreeAsync(en.mem, s);
     cudaEventDestroy(en.ready);
     return err;
   }
