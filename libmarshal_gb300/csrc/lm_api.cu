@@ -273,6 +273,7 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   if (buf == nullptr) return fail("null buffer");
   if (misaligned(buf, e)) return fail("buffer must be aligned to the element size");
   if (a * B >= 0xffffffffull) return fail("a*B must be < 2^32");
+  widen_units(buf, &e, &b);
   if (m == Method::Auto || m == Method::BS) {
     BsPlan p = plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e);
     if (p.feasible)
@@ -500,6 +501,7 @@ static Method tuned_method(cudaStream_t s, int e, uint64_t T, uint64_t a,
 bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
                       uint64_t a, uint64_t B, uint64_t b, int tune) {
   Method m = Method::Auto;
+  if (valid_e(e)) widen_units(buf, &e, &b);  // the tuned class is the wide one
   if (tune && valid_e(e) && T > 0 && a > 1 && B > 1 && b > 0 &&
       T * a * B * b * (uint64_t)e >= (1ull << 20)) {
     m = tuned_method(s, e, T, a, B, b);

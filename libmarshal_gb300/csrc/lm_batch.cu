@@ -921,6 +921,7 @@ static uint32_t batch_pitch(uint64_t row_bytes, int e) {
 struct Normalized {
   bool ok = false;
   uint64_t T = 0, a = 0, B = 0, b = 0;
+  int e = 0;  // element bytes (widened by plan_batch where units allow)
 };
 
 // Every op of the library as a 0100(T, a, B, b).
@@ -963,6 +964,7 @@ static Normalized normalize(const lm_job &jb) {
     default:
       return n;
   }
+  n.e = jb.elem_bytes;
   n.ok = true;
   return n;
 }
@@ -1118,7 +1120,7 @@ static uint64_t arena_bytes() {
 static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
                      uint32_t pitch) {
   j.base = (char *)jb.buf;
-  j.e = jb.elem_bytes;
+  j.e = nz.e;
   j.a = (uint32_t)nz.a;
   j.B = (uint32_t)nz.B;
   j.b = (uint32_t)nz.b;
@@ -1145,7 +1147,7 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
 // for the caller.
 static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
                        uint64_t *nblk, size_t *stage_bytes) {
-  const uint64_t unit = nz.b * (uint64_t)jb.elem_bytes;
+  const uint64_t unit = nz.b * (uint64_t)nz.e;
   if (unit > kStageTileBytes || nz.a * nz.B * nz.b >= 0xffffffffull)
     return false;
   uint32_t S = 128;
@@ -1163,7 +1165,7 @@ static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.div_Sb = make_fastdiv(S * (uint32_t)nz.b);
   j.div_nJ = make_fastdiv(j.nJ);
   j.div_nIJ = make_fastdiv(j.nIJ);
-  j.bytes = nz.T * nz.a * nz.B * nz.b * (uint64_t)jb.elem_bytes;
+  j.bytes = nz.T * nz.a * nz.B * nz.b * (uint64_t)nz.e;
   *nblk = nz.T * nI * nJ;
   *stage_bytes = ((size_t)S * sp + 127) / 128 * 128;
   return true;
@@ -1237,18 +1239,23 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
                "batch: job %d: buffer must be aligned to the element size", k);
       return set_error(m);
     }
+    // units move whole: widen the element where the units and the buffer
+    // allow (fewer, wider accesses; the same permutation of bytes)
+    widen_units(jb.buf, &nz.e, &nz.b);
+    bt->norm[k] = nz;
+    const int e = nz.e;
     const uint64_t row_elems = nz.B * nz.b;
     const uint64_t tile_elems = row_elems * nz.a;
-    const uint32_t pitch = batch_pitch(row_elems * jb.elem_bytes, jb.elem_bytes);
+    const uint32_t pitch = batch_pitch(row_elems * e, e);
     const uint64_t tile_smem = (uint64_t)pitch * nz.a;
     if (tile_elems >= 0xffffffffull || tile_smem > kSmallItem) {
       uint32_t band = 0, bpitch = 0;
       bool two_per_sm = false;
       int gi = (flags & LM_BATCH_NO_CLUSTER)
                    ? -1
-                   : band_group(nz.a, nz.B, nz.b, jb.elem_bytes, band_budget,
+                   : band_group(nz.a, nz.B, nz.b, e, band_budget,
                                 band_half, &band, &bpitch, &two_per_sm);
-      const uint64_t unit = nz.b * (uint64_t)jb.elem_bytes;
+      const uint64_t unit = nz.b * (uint64_t)e;
       const uint64_t foot = (bytes + 255) / 256 * 256 + 256;
       const bool stageable = foot <= arena_cap && unit <= kStageTileBytes &&
                              tile_elems < 0xffffffffull;
@@ -1296,7 +1303,7 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
       // staged form's 4) goes to the planner
       if (nz.T == 1 && unit < 128 && bytes >= kStashPreferBytes &&
           nz.a >= 16ull * (uint64_t)di.sms && nz.a * nz.B >= (1ull << 20) &&
-          plan_stash(nz.a, nz.B, (uint32_t)nz.b, jb.elem_bytes).feasible)
+          plan_stash(nz.a, nz.B, (uint32_t)nz.b, e).feasible)
         goto planner;
       // staged: the job fits the arena (in the current wave or a new one)
       if (stageable) {
@@ -1456,6 +1463,7 @@ bool staged0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
   jb.elem_bytes = e;
   Normalized nz;
   nz.ok = true;
+  nz.e = e;
   nz.T = T;
   nz.a = a;
   nz.B = B;
@@ -1478,6 +1486,7 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
   jb.elem_bytes = e;
   Normalized nz;
   nz.ok = true;
+  nz.e = e;
   nz.T = T;
   nz.a = a;
   nz.B = B;
@@ -1615,7 +1624,7 @@ static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   std::vector<uint32_t> order(bt->large);
   auto bytes_of = [&](uint32_t k) {
     const Normalized &nz = bt->norm[k];
-    return nz.T * nz.a * nz.B * nz.b * (uint64_t)jobs[k].elem_bytes;
+    return nz.T * nz.a * nz.B * nz.b * (uint64_t)nz.e;
   };
   std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
     return bytes_of(x) > bytes_of(y);
@@ -1637,7 +1646,7 @@ static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
     load[best] += bytes_of(k);
     const cudaStream_t qs = nside > 1 ? bt->side[best] : s;
     const Normalized &nz = bt->norm[k];
-    if (run_0100_planned(qs, jobs[k].buf, jobs[k].elem_bytes, nz.T, nz.a,
+    if (run_0100_planned(qs, jobs[k].buf, nz.e, nz.T, nz.a,
                          nz.B, nz.b, (flags & LM_BATCH_NO_TUNE) ? 0 : 1))
       return true;
   }

@@ -129,6 +129,21 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
                               uint64_t a, uint64_t B, uint64_t b,
                               void *scratch);
 
+// A 0100 moves whole units of b elements, so the same byte permutation is a
+// 0100 over elements of any width w dividing the unit's b*e bytes.  Widens
+// *e to the largest such w up to 8 that also divides the buffer address, and
+// rescales *b (fewer, wider accesses in every kernel); b == 1 is unchanged.
+inline void widen_units(const void *buf, int *e, uint64_t *b) {
+  if (*b <= 1) return;
+  const uint64_t U = *b * (uint64_t)*e;
+  int w = 8;
+  while (w > *e && (U % (uint64_t)w || (uintptr_t)buf % (uintptr_t)w)) w >>= 1;
+  if (w > *e) {
+    *b = U / (uint64_t)w;
+    *e = w;
+  }
+}
+
 // An LM_OP_* with its dimensions as the 0100(T, a, B, b) it performs; false
 // for an unknown op or bad dimensions (lm_batch.cu).
 bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
