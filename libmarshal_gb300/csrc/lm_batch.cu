@@ -42,6 +42,9 @@ constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
 // form (the stash moves 3 x payload, the staged form 4 x)
 constexpr uint64_t kStashPreferBytes = 64ull << 20;
 constexpr int kSideStreams = 5;      // streams of the large jobs and groups
+// jobs at least this large that the 16-byte tile kernel applies to run as
+// launches of their own
+constexpr uint64_t kTile010PreferBytes = 2ull << 20;
 
 struct BJob {
   char *base;
@@ -88,43 +91,6 @@ __device__ __forceinline__ void copy_job(BJob *dst, const BJob *src) {
   for (uint32_t k = lane; k < sizeof(BJob) / 4; k += 32)
     reinterpret_cast<uint32_t *>(dst)[k] =
         reinterpret_cast<const uint32_t *>(src)[k];
-}
-
-// Element k (a compile-time index after unrolling) of a 16-byte vector, and
-// its replacement, for E-byte elements.
-template <int E>
-__device__ __forceinline__ typename Elem<E>::T vec_elem(const uint4 &x,
-                                                        uint32_t k) {
-  const uint32_t w = k * E / 4;  // 32-bit word holding the element
-  const uint32_t word = w == 0 ? x.x : w == 1 ? x.y : w == 2 ? x.z : x.w;
-  if (E == 8) {
-    const uint32_t hi = w == 0 ? x.y : w == 2 ? x.w : 0u;
-    return (typename Elem<E>::T)(((uint64_t)hi << 32) | word);
-  }
-  if (E == 4) return (typename Elem<E>::T)word;
-  const uint32_t sh = (k * E % 4) * 8;
-  return (typename Elem<E>::T)(word >> sh);
-}
-
-template <int E>
-__device__ __forceinline__ void vec_set(uint4 &x, uint32_t k,
-                                        typename Elem<E>::T v) {
-  const uint32_t w = k * E / 4;
-  uint32_t *p = w == 0 ? &x.x : w == 1 ? &x.y : w == 2 ? &x.z : &x.w;
-  if (E == 8) {
-    const uint64_t v64 = (uint64_t)v;
-    *p = (uint32_t)v64;
-    if (w == 0) x.y = (uint32_t)(v64 >> 32);
-    else x.w = (uint32_t)(v64 >> 32);
-    return;
-  }
-  if (E == 4) {
-    *p = (uint32_t)v;
-    return;
-  }
-  const uint32_t sh = (k * E % 4) * 8;
-  const uint32_t mask = (E == 1 ? 0xffu : 0xffffu) << sh;
-  *p = (*p & ~mask) | (((uint32_t)v << sh) & mask);
 }
 
 // One item: `ntiles` whole tiles, a contiguous range of the job's buffer.
@@ -1248,6 +1214,16 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
     const uint64_t tile_elems = row_elems * nz.a;
     const uint32_t pitch = batch_pitch(row_elems * e, e);
     const uint64_t tile_smem = (uint64_t)pitch * nz.a;
+    // a large job of one-element units in small tiles runs as its own
+    // launch of the 16-byte tile kernel (on a side stream, beside the rest)
+    if (nz.b == 1 && bytes >= kTile010PreferBytes &&
+        tile010_applies(jb.buf, e, nz.T, nz.a, nz.B) &&
+        !getenv("LM_NO_TILE010")) {
+      bt->large.push_back((uint32_t)k);
+      bt->stats.large_jobs += 1;
+      bt->stats.large_bytes += bytes;
+      continue;
+    }
     if (tile_elems >= 0xffffffffull || tile_smem > kSmallItem) {
       uint32_t band = 0, bpitch = 0;
       bool two_per_sm = false;

@@ -366,6 +366,10 @@ cudaError_t launch_bs0100(cudaStream_t s, void *buf, int e, uint64_t T,
                           const BsPlan &p) {
   if (!p.feasible) return cudaErrorInvalidValue;
   if (T == 0 || a <= 1 || B <= 1) return cudaSuccess;  // empty or identity
+  // single-element units in small tiles: the 16-byte form (lm_tile010.cu)
+  if (b == 1 && p.cluster == 1 && tile010_applies(buf, e, T, a, B) &&
+      !getenv("LM_NO_TILE010"))
+    return launch_tile010(s, buf, e, T, a, B);
   BsArgs g;
   g.base = reinterpret_cast<char *>(buf);
   g.T = T;

@@ -64,6 +64,43 @@ template <> struct Elem<2> { using T = unsigned short; };
 template <> struct Elem<4> { using T = unsigned int; };
 template <> struct Elem<8> { using T = unsigned long long; };
 
+// Element k (a compile-time index after unrolling) of a 16-byte vector, and
+// its replacement, for E-byte elements.
+template <int E>
+__device__ __forceinline__ typename Elem<E>::T vec_elem(const uint4 &x,
+                                                        uint32_t k) {
+  const uint32_t w = k * E / 4;  // 32-bit word holding the element
+  const uint32_t word = w == 0 ? x.x : w == 1 ? x.y : w == 2 ? x.z : x.w;
+  if (E == 8) {
+    const uint32_t hi = w == 0 ? x.y : w == 2 ? x.w : 0u;
+    return (typename Elem<E>::T)(((uint64_t)hi << 32) | word);
+  }
+  if (E == 4) return (typename Elem<E>::T)word;
+  const uint32_t sh = (k * E % 4) * 8;
+  return (typename Elem<E>::T)(word >> sh);
+}
+
+template <int E>
+__device__ __forceinline__ void vec_set(uint4 &x, uint32_t k,
+                                        typename Elem<E>::T v) {
+  const uint32_t w = k * E / 4;
+  uint32_t *p = w == 0 ? &x.x : w == 1 ? &x.y : w == 2 ? &x.z : &x.w;
+  if (E == 8) {
+    const uint64_t v64 = (uint64_t)v;
+    *p = (uint32_t)v64;
+    if (w == 0) x.y = (uint32_t)(v64 >> 32);
+    else x.w = (uint32_t)(v64 >> 32);
+    return;
+  }
+  if (E == 4) {
+    *p = (uint32_t)v;
+    return;
+  }
+  const uint32_t sh = (k * E % 4) * 8;
+  const uint32_t mask = (E == 1 ? 0xffu : 0xffffu) << sh;
+  *p = (*p & ~mask) | (((uint32_t)v << sh) & mask);
+}
+
 // Coherent (L2) 32-bit load with relaxed gpu-scope semantics.
 __device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t *p) {
   uint32_t v;
@@ -146,6 +183,13 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// Waits until at most N of this thread's committed cp.async groups are
+// still pending.
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // Waits for all of this thread's committed cp.async groups.

@@ -57,6 +57,14 @@ cudaError_t launch_bs0100(cudaStream_t s, void *buf, int e, uint64_t T,
                           uint32_t a, uint32_t B, uint32_t b,
                           const BsPlan &plan);
 
+// ---- 010 tiles with 16-byte accesses (lm_tile010.cu) ----------------------
+// [T][a][B] -> [T][B][a] for a 16-byte aligned buffer whose tiles hold at
+// most 32 KB and have a*e or B*e a multiple of 16 bytes.
+bool tile010_applies(const void *buf, int e, uint64_t T, uint64_t a,
+                     uint64_t B);
+cudaError_t launch_tile010(cudaStream_t s, void *buf, int e, uint64_t T,
+                           uint32_t a, uint32_t B);
+
 // ---- 0100 by cycle following with done-bits in global memory -------------
 // A instances of 100(a, B, b): units of b*e bytes; one done bit per unit.
 // `flags` must hold pttwac_flag_bytes(...) zeroed bytes.

@@ -1,0 +1,242 @@
+// lm_tile010.cu -- 010 tiles [a][B] -> [B][a] of 1..8-byte elements with
+// 16-byte global accesses on both sides.
+//
+// Reference algorithm: the BS form of the in-tile transposition (stage a
+// tile on chip, write it back transposed; src/cl/cl_aos_asta.cl:53-161).
+// With narrow elements the element-wise form (k_bs0100: one load, one
+// shared store, one shared load and one store per element) is bound by
+// instruction issue, not by HBM.  Here every global access is a 16-byte
+// vector and each element costs one shared-memory access plus a byte-lane
+// insert or extract:
+//  * form A, a*e a multiple of 16 (every output row is whole vectors; the
+//    AoS -> ASTA conversions): the chunk lands unchanged in shared memory;
+//    a thread builds one output vector from 16/e consecutive rows of one
+//    column -- lanes on consecutive columns, so the shared reads are free
+//    of bank conflicts -- and stores it;
+//  * form B, B*e a multiple of 16 (every input row is whole vectors; the
+//    ASTA -> AoS conversions): rows land at a pitch of an odd number of
+//    16-byte words; a thread reads one 16-byte piece of a row -- lanes on
+//    consecutive rows -- and writes its elements into the chunk's output
+//    image in shared memory, which is then stored with 16-byte vectors.
+// A CTA walks chunks of whole tiles (about 16 KB) with two input stages:
+// the 16-byte cp.async copies of the next chunk are in flight while the
+// current one is written.  A chunk's output range is its own input range,
+// so CTAs need no ordering.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
+#include "lm_core.cuh"
+#include "lm_internal.h"
+
+namespace lm {
+
+constexpr int kT010Threads = 256;
+constexpr uint32_t kT010Chunk = 16 * 1024;     // target input bytes per chunk
+constexpr uint32_t kT010MaxTile = 32 * 1024;   // larger tiles: k_bs0100
+
+struct T010Args {
+  char *base;        // 16-byte aligned
+  uint64_t T;        // tiles
+  uint64_t nchunks;  // ceil(T / k)
+  uint32_t a, B, k;  // rows and row elements of a tile, tiles per chunk
+  uint32_t R, P;     // row bytes (B*e); staged row pitch (form B)
+  uint32_t tile_bytes;
+  uint32_t stage;    // shared bytes of one input stage
+  FastDiv div_B;     // form A: output vectors -> (column, row block)
+  FastDiv div_NA;    // form A: a*e/16 vectors per output row
+  FastDiv div_a;     // form B: staged row -> (tile, row)
+  FastDiv div_NC;    // form B: R/16 pieces per input row
+  FastDiv div_rows;  // form B: k*a rows of a full chunk
+};
+
+// 16/E elements at p, p + R, p + 2R, ... packed into one 16-byte vector.
+template <int E>
+__device__ __forceinline__ uint4 gather_column(const unsigned char *p,
+                                               uint32_t R) {
+  uint4 v;
+  if (E == 1) {
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t x0 = p[(4 * q + 0) * R], x1 = p[(4 * q + 1) * R];
+      const uint32_t x2 = p[(4 * q + 2) * R], x3 = p[(4 * q + 3) * R];
+      w[q] = __byte_perm(__byte_perm(x0, x1, 0x0040), __byte_perm(x2, x3, 0x0040),
+                         0x5410);
+    }
+    v = make_uint4(w[0], w[1], w[2], w[3]);
+  } else if (E == 2) {
+    const unsigned short *s = reinterpret_cast<const unsigned short *>(p);
+    const uint32_t h = R / 2;
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      w[q] = __byte_perm((uint32_t)s[(2 * q) * h], (uint32_t)s[(2 * q + 1) * h],
+                         0x5410);
+    v = make_uint4(w[0], w[1], w[2], w[3]);
+  } else if (E == 4) {
+    v.x = *reinterpret_cast<const uint32_t *>(p);
+    v.y = *reinterpret_cast<const uint32_t *>(p + R);
+    v.z = *reinterpret_cast<const uint32_t *>(p + 2 * R);
+    v.w = *reinterpret_cast<const uint32_t *>(p + 3 * R);
+  } else {
+    const uint2 lo = *reinterpret_cast<const uint2 *>(p);
+    const uint2 hi = *reinterpret_cast<const uint2 *>(p + R);
+    v = make_uint4(lo.x, lo.y, hi.x, hi.y);
+  }
+  return v;
+}
+
+// All threads: 16-byte cp.async copies of chunk c into `buf` (rows at pitch
+// P when PAD, else unchanged), one commit group.
+template <bool PAD>
+__device__ __forceinline__ void t010_issue(const T010Args &g, uint64_t c,
+                                           unsigned char *buf) {
+  const uint32_t nt = (uint32_t)min64(g.k, g.T - c * g.k);
+  const uint32_t nv = nt * (g.tile_bytes / 16);
+  const char *src = g.base + c * g.k * (uint64_t)g.tile_bytes;
+  for (uint32_t v = threadIdx.x; v < nv; v += kT010Threads) {
+    uint32_t off = v * 16;
+    if (PAD) {
+      const uint32_t row = fdiv(v, g.div_NC);
+      off = row * g.P + (v - row * (g.R / 16)) * 16;
+    }
+    cp_async16(buf + off, src + (uint64_t)v * 16);
+  }
+  cp_async_commit();
+}
+
+template <int E, bool FORM_B>
+__global__ void __launch_bounds__(kT010Threads) k_tile010(T010Args g) {
+  using T = typename Elem<E>::T;
+  constexpr uint32_t VE = 16 / E;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *img = smem + 2 * (size_t)g.stage;  // form B output image
+  if (blockIdx.x >= g.nchunks) return;
+  t010_issue<FORM_B>(g, blockIdx.x, smem);
+  for (uint64_t c = blockIdx.x, n = 0;; c += gridDim.x, ++n) {
+    const unsigned char *cur = smem + (n & 1) * (size_t)g.stage;
+    const uint64_t cn = c + gridDim.x;
+    const bool more = cn < g.nchunks;
+    if (more) {
+      // the other stage was last read before the previous pass's barrier
+      t010_issue<FORM_B>(g, cn, smem + ((n & 1) ^ 1) * (size_t)g.stage);
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_all();
+    }
+    __syncthreads();  // chunk c staged by every thread's copies
+    const uint32_t nt = (uint32_t)min64(g.k, g.T - c * g.k);
+    char *dst = g.base + c * g.k * (uint64_t)g.tile_bytes;
+    if (!FORM_B) {
+      const uint32_t NA = g.a / VE;
+      const uint32_t nvec = nt * g.B * NA;
+      const uint32_t orow = g.a * E;  // output row bytes
+      for (uint32_t x = threadIdx.x; x < nvec; x += kT010Threads) {
+        const uint32_t q = fdiv(x, g.div_B);
+        const uint32_t jj = x - q * g.B;
+        const uint32_t t = fdiv(q, g.div_NA);
+        const uint32_t ib = q - t * NA;
+        const uint32_t tb = t * g.tile_bytes;
+        const uint4 v = gather_column<E>(cur + tb + ib * VE * g.R + jj * E, g.R);
+        __stcg(reinterpret_cast<uint4 *>(dst + tb + jj * orow + ib * 16), v);
+      }
+    } else {
+      const uint32_t rows = nt * g.a;
+      const FastDiv dr = nt == g.k ? g.div_rows : make_fastdiv(rows);
+      const uint32_t NC = g.R / 16;
+      const uint32_t units = rows * NC;
+      const uint32_t ostep = g.a * E;  // output row bytes
+      for (uint32_t x = threadIdx.x; x < units; x += kT010Threads) {
+        const uint32_t pc = fdiv(x, dr);
+        const uint32_t gi = x - pc * rows;
+        const uint32_t t = fdiv(gi, g.div_a);
+        const uint32_t i = gi - t * g.a;
+        const uint4 v = *reinterpret_cast<const uint4 *>(cur + gi * g.P + pc * 16);
+        unsigned char *o = img + t * g.tile_bytes + (pc * VE * g.a + i) * E;
+#pragma unroll
+        for (uint32_t k = 0; k < VE; ++k)
+          *reinterpret_cast<T *>(o + k * ostep) = vec_elem<E>(v, k);
+      }
+      __syncthreads();  // the output image is complete
+      const uint32_t nv = nt * (g.tile_bytes / 16);
+      for (uint32_t v = threadIdx.x; v < nv; v += kT010Threads)
+        __stcg(reinterpret_cast<uint4 *>(dst) + v,
+               *reinterpret_cast<const uint4 *>(img + (size_t)v * 16));
+    }
+    __syncthreads();  // stage and image free for the next pass
+    if (!more) break;
+  }
+}
+
+// --- host side ---------------------------------------------------------------
+
+bool tile010_applies(const void *buf, int e, uint64_t T, uint64_t a,
+                     uint64_t B) {
+  if (e != 1 && e != 2 && e != 4 && e != 8) return false;
+  if (T == 0 || a < 2 || B < 2 || ((uintptr_t)buf & 15)) return false;
+  const uint64_t tile = a * B * (uint64_t)e;
+  if (tile > kT010MaxTile) return false;
+  return (a * e) % 16 == 0 || (B * e) % 16 == 0;
+}
+
+template <int E, bool FORM_B>
+static cudaError_t run_tile010(cudaStream_t s, const T010Args &g,
+                               size_t smem) {
+  auto kern = k_tile010<E, FORM_B>;
+  cudaError_t err = cudaFuncSetAttribute(
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int occ = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kT010Threads,
+                                                      smem);
+  if (err != cudaSuccess) return err;
+  uint64_t blocks = (uint64_t)device_info().sms * std::max(occ, 1);
+  if (g.nchunks < blocks) blocks = g.nchunks;
+  if (getenv("LM_VERBOSE"))
+    fprintf(stderr, "tile010: form %c e=%d k=%u stage=%u smem=%zu occ=%d "
+            "blocks=%llu chunks=%llu\n", FORM_B ? 'B' : 'A', E, g.k, g.stage,
+            smem, occ, (unsigned long long)blocks,
+            (unsigned long long)g.nchunks);
+  ProfScope ps(s, "tile010");
+  kern<<<(unsigned)blocks, kT010Threads, smem, s>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile010(cudaStream_t s, void *buf, int e, uint64_t T,
+                           uint32_t a, uint32_t B) {
+  if (!tile010_applies(buf, e, T, a, B)) return cudaErrorInvalidValue;
+  T010Args g;
+  g.base = reinterpret_cast<char *>(buf);
+  g.T = T;
+  g.a = a;
+  g.B = B;
+  g.R = B * (uint32_t)e;
+  g.tile_bytes = a * g.R;
+  const bool form_b = (a * (uint32_t)e) % 16 != 0;  // form A when both apply
+  g.k = (uint32_t)std::min<uint64_t>(
+      T, std::max<uint32_t>(1, kT010Chunk / g.tile_bytes));
+  g.nchunks = (T + g.k - 1) / g.k;
+  g.P = g.R;
+  if (form_b && ((g.P / 16) & 1) == 0) g.P += 16;  // odd 16-byte words
+  g.stage = ((form_b ? g.k * a * g.P : g.k * g.tile_bytes) + 127) / 128 * 128;
+  const size_t img = form_b ? (size_t)g.k * g.tile_bytes : 0;
+  const size_t smem = 2 * (size_t)g.stage + img;
+  g.div_B = make_fastdiv(B);
+  g.div_NA = make_fastdiv(std::max<uint32_t>(1, a * (uint32_t)e / 16));
+  g.div_a = make_fastdiv(a);
+  g.div_NC = make_fastdiv(std::max<uint32_t>(1, g.R / 16));
+  g.div_rows = make_fastdiv(g.k * a);
+  switch (e) {
+    case 1: return form_b ? run_tile010<1, true>(s, g, smem)
+                          : run_tile010<1, false>(s, g, smem);
+    case 2: return form_b ? run_tile010<2, true>(s, g, smem)
+                          : run_tile010<2, false>(s, g, smem);
+    case 4: return form_b ? run_tile010<4, true>(s, g, smem)
+                          : run_tile010<4, false>(s, g, smem);
+    default: return form_b ? run_tile010<8, true>(s, g, smem)
+                           : run_tile010<8, false>(s, g, smem);
+  }
+}
+
+}  // namespace lm

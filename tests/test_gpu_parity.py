@@ -448,3 +448,43 @@ def test_staged_method_shapes(L, e):
         got = view.cpu().numpy().view(O.DTYPES[e])
         assert np.array_equal(got, O.t0100(src, T, a, B, b)), (T, a, B, b, e)
     assert L.lib().lm_device_status(None) == 0
+
+
+TILE010_SHAPES = [
+    # (T, a, B): a*e or B*e a multiple of 16 bytes selects the 16-byte
+    # tile form (form A: output rows whole vectors; form B: input rows)
+    (7, 32, 11), (5, 16, 3), (9, 11, 32), (3, 7, 16), (4, 16, 5),
+    (3, 5, 2), (6, 2, 9), (40, 64, 3), (2, 3, 16), (1000, 16, 4),
+    (1, 64, 200), (2049, 32, 7), (777, 13, 64), (3, 512, 16), (5, 16, 512),
+]
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_tile010_forms(L, e):
+    """010 on 16-byte aligned buffers through the 16-byte tile kernel (both
+    forms, ragged last chunk, one-tile and many-tile cases) and with it
+    switched off (the element-wise tile kernel), against the oracle."""
+    import torch
+    for (T, a, B) in TILE010_SHAPES:
+        if a * B * e > 32 * 1024:
+            continue
+        n = T * a * B
+        src = O.random_bits(n, e, T + a + B)
+        want = O.t010(src, T, a, B)
+        d = to_dev(src)
+        assert d.data_ptr() % 16 == 0
+        L.transpose_010_bs(d, T, a, B, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), want), (T, a, B, e)
+        # the same through the conversion entry points (AoS -> ASTA is
+        # 010(h/t, t, w); ASTA -> AoS is 010(h/t, w, t))
+        d = to_dev(src)
+        L.aos_asta_bs(d, T * a, B, a, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), want), ("aos", T, a, B, e)
+        os.environ["LM_NO_TILE010"] = "1"
+        try:
+            d = to_dev(src)
+            L.transpose_010_bs(d, T, a, B, elem_bytes=e)
+            assert np.array_equal(from_dev(d, e), want), ("off", T, a, B, e)
+        finally:
+            del os.environ["LM_NO_TILE010"]
+    assert L.lib().lm_device_status(None) == 0
