@@ -33,7 +33,7 @@ namespace lm {
 
 constexpr int kT010Threads = 256;
 constexpr uint32_t kT010Chunk = 16 * 1024;     // target input bytes per chunk
-constexpr uint32_t kT010MaxTile = 32 * 1024;   // larger tiles: k_bs0100
+constexpr uint32_t kT010MaxTile = 64 * 1024;   // larger tiles: k_bs0100
 
 struct T010Args {
   char *base;        // 16-byte aligned
@@ -171,13 +171,45 @@ __global__ void __launch_bounds__(kT010Threads) k_tile010(T010Args g) {
 
 // --- host side ---------------------------------------------------------------
 
-bool tile010_applies(const void *buf, int e, uint64_t T, uint64_t a,
-                     uint64_t B) {
+// Chunk geometry of a 010(T, a, B) on e-byte elements; false when the
+// 16-byte form does not apply (unaligned buffer, no whole-vector side, or
+// a tile too large for two stages in shared memory).
+static bool t010_plan(const void *buf, int e, uint64_t T, uint64_t a,
+                      uint64_t B, T010Args *g, size_t *smem) {
   if (e != 1 && e != 2 && e != 4 && e != 8) return false;
   if (T == 0 || a < 2 || B < 2 || ((uintptr_t)buf & 15)) return false;
   const uint64_t tile = a * B * (uint64_t)e;
   if (tile > kT010MaxTile) return false;
-  return (a * e) % 16 == 0 || (B * e) % 16 == 0;
+  const bool form_a = (a * e) % 16 == 0;  // form A when both apply
+  if (!form_a && (B * e) % 16 != 0) return false;
+  g->base = reinterpret_cast<char *>(const_cast<void *>(buf));
+  g->T = T;
+  g->a = (uint32_t)a;
+  g->B = (uint32_t)B;
+  g->R = (uint32_t)(B * e);
+  g->tile_bytes = (uint32_t)tile;
+  g->k = (uint32_t)std::min<uint64_t>(
+      T, std::max<uint64_t>(1, kT010Chunk / tile));
+  g->nchunks = (T + g->k - 1) / g->k;
+  g->P = g->R;
+  if (!form_a && ((g->P / 16) & 1) == 0) g->P += 16;  // odd 16-byte words
+  g->stage = (uint32_t)(((form_a ? (uint64_t)g->k * tile
+                                 : (uint64_t)g->k * a * g->P) + 127) / 128 * 128);
+  *smem = 2 * (size_t)g->stage + (form_a ? 0 : (size_t)g->k * tile);
+  if (*smem > (size_t)device_info().max_smem_optin) return false;
+  g->div_B = make_fastdiv(g->B);
+  g->div_NA = make_fastdiv(std::max<uint32_t>(1, g->a * (uint32_t)e / 16));
+  g->div_a = make_fastdiv(g->a);
+  g->div_NC = make_fastdiv(std::max<uint32_t>(1, g->R / 16));
+  g->div_rows = make_fastdiv(g->k * g->a);
+  return true;
+}
+
+bool tile010_applies(const void *buf, int e, uint64_t T, uint64_t a,
+                     uint64_t B) {
+  T010Args g;
+  size_t smem;
+  return t010_plan(buf, e, T, a, B, &g, &smem);
 }
 
 template <int E, bool FORM_B>
@@ -205,28 +237,10 @@ static cudaError_t run_tile010(cudaStream_t s, const T010Args &g,
 
 cudaError_t launch_tile010(cudaStream_t s, void *buf, int e, uint64_t T,
                            uint32_t a, uint32_t B) {
-  if (!tile010_applies(buf, e, T, a, B)) return cudaErrorInvalidValue;
   T010Args g;
-  g.base = reinterpret_cast<char *>(buf);
-  g.T = T;
-  g.a = a;
-  g.B = B;
-  g.R = B * (uint32_t)e;
-  g.tile_bytes = a * g.R;
-  const bool form_b = (a * (uint32_t)e) % 16 != 0;  // form A when both apply
-  g.k = (uint32_t)std::min<uint64_t>(
-      T, std::max<uint32_t>(1, kT010Chunk / g.tile_bytes));
-  g.nchunks = (T + g.k - 1) / g.k;
-  g.P = g.R;
-  if (form_b && ((g.P / 16) & 1) == 0) g.P += 16;  // odd 16-byte words
-  g.stage = ((form_b ? g.k * a * g.P : g.k * g.tile_bytes) + 127) / 128 * 128;
-  const size_t img = form_b ? (size_t)g.k * g.tile_bytes : 0;
-  const size_t smem = 2 * (size_t)g.stage + img;
-  g.div_B = make_fastdiv(B);
-  g.div_NA = make_fastdiv(std::max<uint32_t>(1, a * (uint32_t)e / 16));
-  g.div_a = make_fastdiv(a);
-  g.div_NC = make_fastdiv(std::max<uint32_t>(1, g.R / 16));
-  g.div_rows = make_fastdiv(g.k * a);
+  size_t smem = 0;
+  if (!t010_plan(buf, e, T, a, B, &g, &smem)) return cudaErrorInvalidValue;
+  const bool form_b = (a * (uint32_t)e) % 16 != 0;
   switch (e) {
     case 1: return form_b ? run_tile010<1, true>(s, g, smem)
                           : run_tile010<1, false>(s, g, smem);
