@@ -53,11 +53,12 @@ struct BJob {
   uint32_t row_elems, aB, tile_elems, pitch;
   FastDiv div_row, div_b, div_aB, div_a;
   uint32_t band;  // cluster form: units per CTA band (pitch = band pitch)
-  // staged form: S x S unit blocks, nI x nJ of them per tile, written
-  // transposed to `scratch` and copied back
+  // staged form: blocks of S rows x Sj units, nI x nJ of them per tile,
+  // written transposed to `scratch` and copied back; nv16 = units of whole
+  // 16-byte vectors (every row and output run 16-byte aligned), else 0
   char *scratch;
-  uint32_t S, nJ, nIJ;
-  FastDiv div_Sb, div_nJ, div_nIJ;
+  uint32_t S, Sj, nJ, nIJ, nv16;
+  FastDiv div_Sb, div_nJ, div_nIJ, div_S, div_nv16;
   uint64_t bytes;
   // b == 1 stores: groups of 8 staged rows (ceil(a/8) for bands, S/8 for
   // staged blocks)
@@ -607,8 +608,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
 // kernel copies the arena back over the job's buffer.  Items are runs of
 // blocks (gather) or of 16-byte vectors (copy back).
 constexpr int kStageThreads = 256;
-constexpr uint32_t kStageTileBytes = 32 * 1024;  // S*S*b*e at most
-constexpr uint32_t kStageMaxS = 128;
+constexpr uint32_t kStageTileBytes = 32 * 1024;  // staged bytes per block
+constexpr uint32_t kStageMaxS = 256;             // rows per block
 constexpr uint32_t kStageBlocksPerItem = 16;
 constexpr uint64_t kCopyVecsPerItem = 16384;     // 256 KB
 
@@ -624,9 +625,9 @@ __device__ __forceinline__ GBlock gather_decode(const BJob &j, uint32_t q) {
   const uint32_t bi = fdiv(r, j.div_nJ);
   const uint32_t bj = r - bi * j.nJ;
   k.i0 = bi * j.S;
-  k.j0 = bj * j.S;
+  k.j0 = bj * j.Sj;
   k.si = min(j.S, j.a - k.i0);
-  k.sj = min(j.S, j.B - k.j0);
+  k.sj = min(j.Sj, j.B - k.j0);
   return k;
 }
 
@@ -672,6 +673,30 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
   const GBlock k = gather_decode(j, q);
   T *dst = reinterpret_cast<T *>(j.scratch) + (uint64_t)k.t * j.tile_elems +
            ((uint64_t)k.j0 * j.a + k.i0) * j.b;
+  if (j.nv16) {
+    // whole 16-byte vectors: lanes on consecutive vectors of a column's
+    // output run (consecutive staged rows: distinct bank groups)
+    const uint32_t NS = j.nv16, U = NS * 16;
+    const uint32_t n = k.sj * k.si * NS;
+    const FastDiv dsi = k.si == j.S ? j.div_S : make_fastdiv(k.si);
+    unsigned char *d = reinterpret_cast<unsigned char *>(dst);
+    const uint64_t ostride = (uint64_t)j.a * U;  // bytes between output rows
+    for (uint32_t x = threadIdx.x; x < n; x += kStageThreads) {
+      uint32_t u = x, sv = 0;
+      if (NS != 1) {
+        u = fdiv(x, j.div_nv16);
+        sv = x - u * NS;
+      }
+      const uint32_t jj = fdiv(u, dsi);
+      const uint32_t ii = u - jj * k.si;
+      const uint4 v = *reinterpret_cast<const uint4 *>(buf + rowoff[ii] +
+                                                       jj * U + sv * 16);
+      __stcg(reinterpret_cast<uint4 *>(d + (uint64_t)jj * ostride +
+                                       (ii * NS + sv) * 16),
+             v);
+    }
+    return;
+  }
   if (j.b == 1) {
     store_b1<E>(buf, rowoff, k.si, k.sj, j.ng8, j.div_ng8, dst, j.a,
                 threadIdx.x >> 5, kStageThreads / 32);
@@ -1102,28 +1127,57 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.ng8 = (uint32_t)((nz.a + 7) / 8);
   j.div_ng8 = make_fastdiv(j.ng8);
   j.scratch = nullptr;
-  j.S = j.nJ = j.nIJ = 0;
+  j.S = j.Sj = j.nJ = j.nIJ = j.nv16 = 0;
   j.bytes = 0;
 }
 
-// Staged form of a job: S x S unit blocks (S the largest power of two up to
-// 128 with S*S units in kStageTileBytes), rows staged as 16-byte aligned
-// supersets at an odd number of 16-byte words.  False when a unit exceeds
-// kStageTileBytes or the job has 2^32 blocks or more.  `scratch` is left
-// for the caller.
+// Staged form of a job: blocks of S rows x Sj units, rows staged as 16-byte
+// aligned supersets at an odd number of 16-byte words, at most
+// kStageTileBytes per block: whole rows when a row is short (tall, narrow
+// matrices), whole columns when the rows are few (short, wide ones), else
+// S x S with S the largest power of two up to 128 that fits.  False when a
+// unit exceeds kStageTileBytes or the job has 2^32 blocks or more.
+// `scratch` is left for the caller.
 static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
                        uint64_t *nblk, size_t *stage_bytes) {
   const uint64_t unit = nz.b * (uint64_t)nz.e;
   if (unit > kStageTileBytes || nz.a * nz.B * nz.b >= 0xffffffffull)
     return false;
-  uint32_t S = 128;
-  while (S > 1 && (uint64_t)S * S * unit > kStageTileBytes) S >>= 1;
-  const uint64_t nI = (nz.a + S - 1) / S, nJ = (nz.B + S - 1) / S;
+  auto pitch_of = [&](uint64_t sj) {
+    uint64_t p = (sj * unit + 15) / 16 * 16 + 16;
+    if (((p / 16) & 1) == 0) p += 16;  // rows in distinct bank groups
+    return p;
+  };
+  // whole rows while a block keeps 64 of them (output runs of 64 units);
+  // whole columns while a row segment keeps 128 bytes (input runs)
+  const uint64_t min_sj = std::max<uint64_t>(8, (128 + unit - 1) / unit);
+  uint64_t Si, Sj;
+  if (64 * pitch_of(nz.B) <= kStageTileBytes) {
+    Sj = nz.B;  // whole rows
+    Si = std::min<uint64_t>(kStageMaxS, kStageTileBytes / pitch_of(nz.B));
+  } else if (nz.a <= kStageMaxS &&
+             nz.a * pitch_of(min_sj) <= kStageTileBytes) {
+    Si = nz.a;  // whole columns
+    Sj = (kStageTileBytes / nz.a - 32) / unit;
+    while (Sj > min_sj && nz.a * pitch_of(Sj) > kStageTileBytes) --Sj;
+  } else {
+    uint64_t S = 128;
+    while (S > 1 && S * S * unit > kStageTileBytes) S >>= 1;
+    Si = Sj = S;
+  }
+  Si = std::min<uint64_t>(Si, nz.a);
+  Sj = std::min<uint64_t>(Sj, nz.B);
+  const uint64_t nI = (nz.a + Si - 1) / Si, nJ = (nz.B + Sj - 1) / Sj;
   if (nz.T * nI * nJ >= 0xffffffffull) return false;
-  uint32_t sp = (uint32_t)((S * unit + 15) / 16 * 16 + 16);
-  if (((sp / 16) & 1) == 0) sp += 16;  // rows in distinct bank groups
+  const uint32_t sp = (uint32_t)pitch_of(Sj);
+  const uint32_t S = (uint32_t)Si;
   fill_job(j, jb, nz, sp);
   j.S = S;
+  j.Sj = (uint32_t)Sj;
+  j.div_S = make_fastdiv(S);
+  j.nv16 = (unit % 16 == 0 && ((uintptr_t)jb.buf & 15) == 0)
+               ? (uint32_t)(unit / 16) : 0u;
+  j.div_nv16 = make_fastdiv(j.nv16 ? j.nv16 : 1);
   j.ng8 = (S + 7) / 8;
   j.div_ng8 = make_fastdiv(j.ng8);
   j.nJ = (uint32_t)nJ;
