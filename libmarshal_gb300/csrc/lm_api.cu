@@ -308,9 +308,9 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
                   (unsigned long long)a, (unsigned long long)B,
                   (unsigned)kCycleMaxLen);
   }
-  // the stash wavefront spreads rows over all CTAs: with fewer than 8 rows
-  // per CTA (two per SM) its steps are too small to keep HBM busy
-  const uint64_t stash_min_rows = 16ull * (uint64_t)device_info().sms;
+  // the stash wavefront spreads rows over all CTAs: with too few rows per
+  // SM its steps are too small to keep HBM busy
+  const uint64_t stash_min_rows = kStashRowsPerSm * (uint64_t)device_info().sms;
   const bool want_stash =
       m == Method::Stash ||
       (m == Method::Auto && T == 1 && U < 128 && a * B >= (1ull << 20) &&
@@ -337,10 +337,11 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   // any shape through scratch: block transposes out of place, then a copy
   // back (4 x payload, but every access in whole sectors); falls through
   // when the scratch cannot be had
-  // (units of 128 bytes and more move as whole lines in cycle following,
-  // which needs no scratch and is as fast)
+  // (units of 512 bytes and more move as whole lines in cycle following,
+  // which needs no scratch and is as fast or faster)
   if (m == Method::Staged ||
-      (m == Method::Auto && U < 128 && T * a * B * b * e >= (1ull << 20) &&
+      (m == Method::Auto && U < kStagedMaxUnit &&
+       T * a * B * b * e >= (1ull << 20) &&
        !getenv("LM_NO_STAGED"))) {
     if (staged0100_applies(T, a, B, b, e)) {
       Scratch sc;

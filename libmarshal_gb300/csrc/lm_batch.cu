@@ -1332,9 +1332,13 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
       // a large 100 that the stash plan serves (3 x payload instead of the
       // staged form's 4) goes to the planner
       if (nz.T == 1 && unit < 128 && bytes >= kStashPreferBytes &&
-          nz.a >= 16ull * (uint64_t)di.sms && nz.a * nz.B >= (1ull << 20) &&
+          nz.a >= kStashRowsPerSm * (uint64_t)di.sms &&
+          nz.a * nz.B >= (1ull << 20) &&
           plan_stash(nz.a, nz.B, (uint32_t)nz.b, e).feasible)
         goto planner;
+      // large jobs of units of kStagedMaxUnit bytes and more: cycle
+      // following in the planner (2 x payload) is at least as fast
+      if (unit >= kStagedMaxUnit && bytes >= kStashPreferBytes) goto planner;
       // staged: the job fits the arena (in the current wave or a new one)
       if (stageable) {
         if (bt->nwaves == 0 || wave_used + foot > arena_cap) {

@@ -57,6 +57,14 @@ cudaError_t launch_bs0100(cudaStream_t s, void *buf, int e, uint64_t T,
                           uint32_t a, uint32_t B, uint32_t b,
                           const BsPlan &plan);
 
+// ---- planner thresholds (the per-op planner and the batch executor) ------
+// Measured on GB300 with 256 MB matrices: the staged form (4 x payload
+// through scratch) beats cycle following on units below 512 bytes; the
+// stash (3 x payload) needs about 48 rows per SM to keep its wavefront fed,
+// and below that the staged form is faster.
+constexpr uint64_t kStagedMaxUnit = 512;
+constexpr uint64_t kStashRowsPerSm = 48;
+
 // ---- 010 tiles with 16-byte accesses (lm_tile010.cu) ----------------------
 // [T][a][B] -> [T][B][a] for a 16-byte aligned buffer whose tiles hold at
 // most 32 KB and have a*e or B*e a multiple of 16 bytes.
