@@ -859,8 +859,16 @@ __global__ void __launch_bounds__(kStageThreads) k_batch_copyback(BatchArgs g) {
     const uint4 *vs = reinterpret_cast<const uint4 *>(j.scratch + head);
     uint4 *vd = reinterpret_cast<uint4 *>(j.base + head);
     const uint64_t v1 = min64(it.tile0 + kCopyVecsPerItem, nvec);
-    for (uint64_t v = it.tile0 + threadIdx.x; v < v1; v += kStageThreads)
-      __stcs(vd + v, __ldcs(vs + v));
+    // four independent loads in flight per thread
+    for (uint64_t v = it.tile0 + threadIdx.x; v < v1; v += 4 * kStageThreads) {
+      uint4 x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (v + u * kStageThreads < v1) x[u] = __ldcs(vs + v + u * kStageThreads);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (v + u * kStageThreads < v1) __stcs(vd + v + u * kStageThreads, x[u]);
+    }
     if (it.tile0 == 0) {
       const uint64_t tail0 = head + nvec * 16;
       for (uint64_t x = threadIdx.x; x < head + (j.bytes - tail0);
