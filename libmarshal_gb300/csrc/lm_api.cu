@@ -276,7 +276,13 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   widen_units(buf, &e, &b);
   if (m == Method::Auto || m == Method::BS) {
     BsPlan p = plan_bs0100(T, (uint32_t)a, (uint32_t)B, (uint32_t)b, e);
-    if (p.feasible)
+    // a megabyte or more in fewer tile chunks (or clusters) than SMs leaves
+    // most of the GPU idle: the methods below spread any shape over blocks
+    const uint64_t chunks = (T + p.tiles_per_chunk - 1) / p.tiles_per_chunk;
+    const bool thin = m == Method::Auto &&
+                      T * a * B * b * (uint64_t)e >= (1ull << 20) &&
+                      chunks * (uint64_t)p.cluster < (uint64_t)device_info().sms;
+    if (p.feasible && !thin)
       return check_launch(launch_bs0100(s, buf, e, T, (uint32_t)a,
                                         (uint32_t)B, (uint32_t)b, p),
                           "BS launch");
@@ -344,10 +350,14 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
        T * a * B * b * e >= (1ull << 20) &&
        !getenv("LM_NO_STAGED"))) {
     if (staged0100_applies(T, a, B, b, e)) {
+      // the scratch copy sits at the buffer's address modulo 16, so the
+      // copy back runs in aligned 16-byte vectors
       Scratch sc;
-      if (try_scratch(sc, T * a * B * b * e, s))
-        return check_launch(launch_staged0100(s, buf, e, T, a, B, b, sc.p),
-                            "staged launch");
+      if (try_scratch(sc, T * a * B * b * e + 16, s))
+        return check_launch(
+            launch_staged0100(s, buf, e, T, a, B, b,
+                              (char *)sc.p + ((uintptr_t)buf & 15)),
+            "staged launch");
       if (m == Method::Staged) return fail("staged: no scratch for this size");
     } else if (m == Method::Staged) {
       return fail("staged: units above 32 KB or too many blocks");

@@ -612,6 +612,9 @@ constexpr uint32_t kStageTileBytes = 32 * 1024;  // staged bytes per block
 constexpr uint32_t kStageMaxS = 256;             // rows per block
 constexpr uint32_t kStageBlocksPerItem = 16;
 constexpr uint64_t kCopyVecsPerItem = 16384;     // 256 KB
+// staged jobs up to this size keep their scratch in L2 between the gather
+// and the copy back
+constexpr uint64_t kL2StageBytes = 48ull << 20;
 
 // Block q of a staged job: tile t, block row bi, block column bj.
 struct GBlock {
@@ -876,6 +879,52 @@ __global__ void __launch_bounds__(kStageThreads) k_batch_copyback(BatchArgs g) {
         const uint64_t off = x < head ? x : tail0 + (x - head);
         j.base[off] = j.scratch[off];
       }
+    }
+  }
+}
+
+// Copy back of one staged job whose scratch is still in L2 (written by the
+// gather just before): 16-byte vectors, a warp on 512 consecutive bytes per
+// step, then the scratch lines it has read are dropped from L2 without a
+// write-back (discard), so the staging costs DRAM no traffic of its own.
+// `dst` and `src` have the same address modulo 16; the ragged head and tail
+// bytes are copied by block 0.
+__global__ void __launch_bounds__(kStageThreads) k_stage_copyback(
+    char *dst, const char *src, uint64_t bytes) {
+  const uintptr_t d = (uintptr_t)dst;
+  const uint64_t head = min64((16 - (d & 15)) & 15, bytes);
+  const uint64_t nvec = (bytes - head) / 16;
+  const uint4 *vs = reinterpret_cast<const uint4 *>(src + head);
+  uint4 *vd = reinterpret_cast<uint4 *>(dst + head);
+  // scratch lines wholly inside [src, src + bytes) may be dropped (the
+  // ragged head and tail bytes never lie in one)
+  const uintptr_t l0 = ((uintptr_t)src + 127) & ~(uintptr_t)127;
+  const uintptr_t l1 = ((uintptr_t)src + bytes) & ~(uintptr_t)127;
+  // warps walk 512-byte aligned windows of the scratch: whole lines each
+  const uintptr_t s0 = (uintptr_t)src + head, s1 = s0 + nvec * 16;
+  const uintptr_t w0 = s0 & ~(uintptr_t)511;
+  const uint64_t nwin = nvec ? (s1 - w0 + 511) / 512 : 0;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (kStageThreads / 32);
+  for (uint64_t w = blockIdx.x * (uint64_t)(kStageThreads / 32) +
+                    (threadIdx.x >> 5);
+       w < nwin; w += warps) {
+    const uintptr_t a = w0 + w * 512 + (uintptr_t)lane * 16;
+    if (a >= s0 && a < s1) {
+      const uint64_t v = (a - s0) / 16;
+      __stcs(vd + v, __ldcg(vs + v));
+    }
+    __syncwarp();  // every lane's load from this window has completed
+    const uintptr_t line = w0 + w * 512 + (uintptr_t)lane * 128;
+    if (lane < 4 && line >= l0 && line + 128 <= l1)
+      discard_l2_line((const void *)line);
+  }
+  if (blockIdx.x == 0) {
+    const uint64_t tail0 = head + nvec * 16;
+    for (uint64_t x = threadIdx.x; x < head + (bytes - tail0);
+         x += kStageThreads) {
+      const uint64_t off = x < head ? x : tail0 + (x - head);
+      dst[off] = src[off];
     }
   }
 }
@@ -1563,8 +1612,20 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
     k_batch_gather<<<grid, kStageThreads, dyn, s>>>(g);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
-  return cudaMemcpyAsync(buf, scratch, g.single.bytes, cudaMemcpyDeviceToDevice,
-                         s);
+  if (g.single.bytes > kL2StageBytes ||
+      (((uintptr_t)buf ^ (uintptr_t)scratch) & 15) || getenv("LM_NO_L2STAGE"))
+    return cudaMemcpyAsync(buf, scratch, g.single.bytes,
+                           cudaMemcpyDeviceToDevice, s);
+  // the scratch is still in L2: copy it back and drop it there
+  const uint64_t wins = g.single.bytes / 512 + 2;
+  const uint32_t cgrid = (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>((uint64_t)di.sms * 8,
+                            (wins + kStageThreads / 32 - 1) / (kStageThreads / 32)));
+  ProfScope ps(s, "stage_copyback");
+  k_stage_copyback<<<cgrid, kStageThreads, 0, s>>>(
+      reinterpret_cast<char *>(buf), reinterpret_cast<const char *>(scratch),
+      g.single.bytes);
+  return cudaGetLastError();
 }
 
 }  // namespace lm

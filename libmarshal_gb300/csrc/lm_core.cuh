@@ -101,6 +101,13 @@ __device__ __forceinline__ void vec_set(uint4 &x, uint32_t k,
   *p = (*p & ~mask) | (((uint32_t)v << sh) & mask);
 }
 
+// Drops the 128-byte L2 line at p (128-byte aligned) without writing it
+// back: its contents become undefined.  For scratch that has been read for
+// the last time, so that dirty staging lines never reach DRAM.
+__device__ __forceinline__ void discard_l2_line(const void *p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
 // Coherent (L2) 32-bit load with relaxed gpu-scope semantics.
 __device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t *p) {
   uint32_t v;

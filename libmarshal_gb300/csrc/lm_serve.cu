@@ -436,10 +436,6 @@ bool lm_serve_stats_get(lm_serve_t s, lm_serve_stats *out) {
 // order already keeps reused buffers safe), with the planner's default
 // choice per shape (no autotuning, which would time candidates on first
 // sight of a shape class).
-static void CUDART_CB stamp_now(void *p) {
-  static_cast<std::atomic<int64_t> *>(p)->store(now_ns());
-}
-
 static void wait_until(int64_t t) {
   while (now_ns() < t) std::this_thread::yield();
 }
@@ -456,14 +452,29 @@ bool lm_serve_replay(lm_serve_t s, const lm_request *reqs,
       return lm::set_error("serve replay: after[k] must be -1 or < k");
   const int64_t t0 = now_ns() + 1000000;  // 1 ms to get going
   if (plain) {
+    // completion times from timing events (a host callback per request
+    // would stall the stream for its round trip): request k's completion is
+    // the host time of the start event plus the device time between it and
+    // k's event
     cudaStream_t st;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
       return lm::set_error("serve replay: stream");
-    std::vector<std::atomic<int64_t>> stamps(n);
+    std::vector<cudaEvent_t> ev(n + 1, nullptr);
+    bool ev_ok = true;
+    for (int k = 0; k <= n && ev_ok; ++k)
+      ev_ok = cudaEventCreate(&ev[k]) == cudaSuccess;
+    if (!ev_ok) {
+      for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+      cudaStreamDestroy(st);
+      return lm::set_error("serve replay: events");
+    }
     std::vector<int64_t> t_sub(n);
     std::vector<int> status(n, 0);
+    cudaEventRecord(ev[n], st);
+    cudaEventSynchronize(ev[n]);
+    const int64_t t_ev = now_ns();  // the start event has executed
     for (int k = 0; k < n; ++k) {
-      stamps[k].store(0);
       const lm_request &r = reqs[k];
       uint64_t T, a, B, b;
       wait_until(t0 + arrival_ns[k]);
@@ -472,23 +483,23 @@ bool lm_serve_replay(lm_serve_t s, const lm_request *reqs,
         status[k] = 1;
       else if (lm::run_0100_planned(st, r.buf, r.elem_bytes, T, a, B, b, 0))
         status[k] = 1;
-      if (cudaLaunchHostFunc(st, stamp_now, &stamps[k]) != cudaSuccess) {
-        cudaStreamSynchronize(st);
-        stamps[k].store(now_ns());
-      }
+      cudaEventRecord(ev[k], st);
     }
     cudaStreamSynchronize(st);
-    cudaStreamDestroy(st);
     bool failed = false;
     for (int k = 0; k < n; ++k) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[n], ev[k]);
       const int64_t arr = t0 + arrival_ns[k];
       out[k].ticket = (unsigned long long)k + 1;
       out[k].status = status[k];
-      out[k].done_ns = stamps[k].load();
+      out[k].done_ns = std::max<int64_t>(t_sub[k], t_ev + (int64_t)(ms * 1e6));
       out[k].latency_ns = out[k].done_ns - arr;
       out[k].queue_ns = t_sub[k] - arr;
       failed |= status[k] != 0;
     }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    cudaStreamDestroy(st);
     return failed ? lm::set_error("serve replay: a plain request failed")
                   : false;
   }
