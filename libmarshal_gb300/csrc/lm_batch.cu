@@ -473,6 +473,11 @@ __device__ void band_store(const BJob &j, uint64_t tile, uint32_t rank,
   const uint32_t n = j.a * (p.len / E);
   T *dst = reinterpret_cast<T *>(j.base) + tile * (uint64_t)j.tile_elems +
            (uint64_t)p.bc0 * j.a * j.b;
+  if (E <= 4 && j.b == 1 && (j.a * E) % 16 == 0 && ((uintptr_t)dst & 15) == 0) {
+    store_columns16<E>(buf, rowoff, j.a, p.len / E,
+                       reinterpret_cast<unsigned char *>(dst), t, nt);
+    return;
+  }
   if (j.b == 1) {
     store_b1<E>(buf, rowoff, j.a, p.len / E, j.ng8, j.div_ng8, dst, j.a,
                 t >> 5, nt >> 5);

@@ -207,7 +207,13 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100_band(BsArgs g) {
     // ---- store: output rows bc0..bc1-1 = elements [bc0*a*b, bc1*a*b)
     const uint32_t n = g.a * band_elems;
     T *dst = t + (uint64_t)bc0 * g.a * g.b;
-    if (s_ok) {
+    if (s_ok && E <= 4 && g.b == 1 && (g.a * E) % 16 == 0 &&
+        ((uintptr_t)dst & 15) == 0) {
+      // whole-vector output rows: 16-byte stores
+      store_columns16<E>(smem, rowoff, g.a, nbu,
+                         reinterpret_cast<unsigned char *>(dst), threadIdx.x,
+                         kBsThreads);
+    } else if (s_ok) {
       for (uint32_t base = threadIdx.x; base < n;
            base += kBsThreads * kBsUnroll) {
         T v[kBsUnroll];

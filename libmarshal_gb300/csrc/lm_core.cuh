@@ -101,6 +101,69 @@ __device__ __forceinline__ void vec_set(uint4 &x, uint32_t k,
   *p = (*p & ~mask) | (((uint32_t)v << sh) & mask);
 }
 
+// 16/E elements packed into one 16-byte vector, element 0 in the lowest
+// bytes.
+template <int E>
+__device__ __forceinline__ uint4 pack16(const typename Elem<E>::T (&x)[16 / E]) {
+  if constexpr (E == 1) {
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      w[q] = __byte_perm(__byte_perm(x[4 * q], x[4 * q + 1], 0x0040),
+                         __byte_perm(x[4 * q + 2], x[4 * q + 3], 0x0040),
+                         0x5410);
+    return make_uint4(w[0], w[1], w[2], w[3]);
+  } else if constexpr (E == 2) {
+    return make_uint4(__byte_perm(x[0], x[1], 0x5410),
+                      __byte_perm(x[2], x[3], 0x5410),
+                      __byte_perm(x[4], x[5], 0x5410),
+                      __byte_perm(x[6], x[7], 0x5410));
+  } else if constexpr (E == 4) {
+    return make_uint4(x[0], x[1], x[2], x[3]);
+  } else {
+    return make_uint4((uint32_t)x[0], (uint32_t)(x[0] >> 32), (uint32_t)x[1],
+                      (uint32_t)(x[1] >> 32));
+  }
+}
+
+// Output rows of `ncol` staged columns, `a` elements each, written as 16-byte
+// vectors (a*E a multiple of 16 and dst 16-byte aligned): vector (ib, c)
+// holds rows ib*16/E .. ib*16/E + 16/E - 1 of column c.  Lane pairs take
+// the two vectors of one 32-byte sector of a column (whole-sector stores),
+// pairs on consecutive columns (neighbouring shared addresses; the row
+// offsets are broadcast).  Staged row r starts at buf + rowoff[r], column c
+// of it at + c*E; column c is output row c at dst + c*a*E.  Threads t of nt
+// take part.
+template <int E>
+__device__ __forceinline__ void store_columns16(const unsigned char *buf,
+                                                const uint32_t *rowoff,
+                                                uint32_t a, uint32_t ncol,
+                                                unsigned char *dst, uint32_t t,
+                                                uint32_t nt) {
+  using T = typename Elem<E>::T;
+  constexpr uint32_t VE = 16 / E;
+  if (ncol == 0) return;
+  const uint32_t NA = a / VE;             // vectors per output row
+  const uint32_t G = NA >= 2 ? 2u : 1u;   // vectors of a column per lane group
+  const uint32_t nvec = ((NA + G - 1) / G) * G * ncol;
+  const FastDiv dc = make_fastdiv(ncol);
+  const uint64_t orow = (uint64_t)a * E;
+#pragma unroll 1
+  for (uint32_t x = t; x < nvec; x += nt) {
+    const uint32_t lo = G == 2 ? (x & 1u) : 0u;
+    const uint32_t y = G == 2 ? (x >> 1) : x;
+    const uint32_t hi = fdiv(y, dc);
+    const uint32_t c = y - hi * ncol;
+    const uint32_t ib = hi * G + lo;
+    if (ib >= NA) continue;
+    T v[VE];
+#pragma unroll
+    for (uint32_t k = 0; k < VE; ++k)
+      v[k] = *reinterpret_cast<const T *>(buf + rowoff[ib * VE + k] + c * E);
+    __stcg(reinterpret_cast<uint4 *>(dst + c * orow + ib * 16), pack16<E>(v));
+  }
+}
+
 // Drops the 128-byte L2 line at p (128-byte aligned) without writing it
 // back: its contents become undefined.  For scratch that has been read for
 // the last time, so that dirty staging lines never reach DRAM.
