@@ -276,7 +276,11 @@ BsPlan plan_bs0100(uint64_t T, uint32_t a, uint32_t B, uint32_t b, int e,
     p.tiles_per_chunk = (uint32_t)k;
     p.cluster = 1;
     p.rows_per_cta = (uint32_t)(k * a);
-  } else if (tile_smem <= max_smem) {
+  } else if (tile_smem <= max_smem &&
+             !(b == 1 && e <= 4 && tile_smem > 112 * 1024 &&
+               a <= kBandMaxRows)) {
+    // (one-element units of narrow types in tiles above 112 KB go to the
+    // cluster form, whose bands write 16-byte vectors)
     p.tiles_per_chunk = 1;
     p.cluster = 1;
     p.rows_per_cta = a;

@@ -33,7 +33,7 @@ namespace lm {
 
 constexpr int kT010Threads = 256;
 constexpr uint32_t kT010Chunk = 16 * 1024;     // target input bytes per chunk
-constexpr uint32_t kT010MaxTile = 64 * 1024;   // larger tiles: k_bs0100
+constexpr uint32_t kT010MaxTile = 112 * 1024;  // larger tiles: k_bs0100
 
 struct T010Args {
   char *base;        // 16-byte aligned

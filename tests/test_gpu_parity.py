@@ -457,6 +457,7 @@ TILE010_SHAPES = [
     (3, 5, 2), (6, 2, 9), (40, 64, 3), (2, 3, 16), (1000, 16, 4),
     (1, 64, 200), (2049, 32, 7), (777, 13, 64), (3, 512, 16), (5, 16, 512),
     (4, 64, 700), (3, 700, 64), (2, 1000, 32), (3, 48, 1000),
+    (3, 32, 1700), (2, 1700, 32), (3, 16, 7000),
 ]
 
 
@@ -467,7 +468,7 @@ def test_tile010_forms(L, e):
     switched off (the element-wise tile kernel), against the oracle."""
     import torch
     for (T, a, B) in TILE010_SHAPES:
-        if a * B * e > 64 * 1024:
+        if a * B * e > 112 * 1024:
             continue
         n = T * a * B
         src = O.random_bits(n, e, T + a + B)
