@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
 constexpr int kStageThreads = 256;
 constexpr uint32_t kStageTileBytes = 32 * 1024;  // staged bytes per block
 constexpr uint32_t kStageMaxS = 256;             // rows per block
-constexpr uint32_t kStageBlocksPerItem = 16;
+constexpr uint32_t kStageBlocksPerItem = 4;   // fine-grained: balanced tails
 constexpr uint64_t kCopyVecsPerItem = 16384;     // 256 KB
 // staged jobs up to this size keep their scratch in L2 between the gather
 // and the copy back
