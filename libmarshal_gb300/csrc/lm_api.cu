@@ -279,7 +279,10 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
     // a megabyte or more in fewer tile chunks (or clusters) than SMs leaves
     // most of the GPU idle: the methods below spread any shape over blocks
     const uint64_t chunks = (T + p.tiles_per_chunk - 1) / p.tiles_per_chunk;
-    const bool thin = m == Method::Auto &&
+    // (the 16-byte tile kernel sizes its own chunks to the GPU)
+    const bool t010 = b == 1 && p.feasible && p.cluster == 1 &&
+                      tile010_applies(buf, e, T, a, B);
+    const bool thin = m == Method::Auto && !t010 &&
                       T * a * B * b * (uint64_t)e >= (1ull << 20) &&
                       chunks * (uint64_t)p.cluster < (uint64_t)device_info().sms;
     if (p.feasible && !thin)

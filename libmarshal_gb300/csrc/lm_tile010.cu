@@ -188,8 +188,12 @@ static bool t010_plan(const void *buf, int e, uint64_t T, uint64_t a,
   g->B = (uint32_t)B;
   g->R = (uint32_t)(B * e);
   g->tile_bytes = (uint32_t)tile;
-  g->k = (uint32_t)std::min<uint64_t>(
-      T, std::max<uint64_t>(1, kT010Chunk / tile));
+  // about 16 KB per chunk, but at least two chunks per SM when the tiles
+  // are few (a small op spread over the whole GPU)
+  const uint64_t spread = (T + 2 * (uint64_t)device_info().sms - 1) /
+                          (2 * (uint64_t)device_info().sms);
+  g->k = (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>({T, kT010Chunk / tile, spread}));
   g->nchunks = (T + g->k - 1) / g->k;
   g->P = g->R;
   if (!form_a && ((g->P / 16) & 1) == 0) g->P += 16;  // odd 16-byte words
