@@ -490,3 +490,25 @@ def test_tile010_forms(L, e):
         finally:
             del os.environ["LM_NO_TILE010"]
     assert L.lib().lm_device_status(None) == 0
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_010_unaligned_buffers(L, e):
+    """010 on a buffer that is only element-aligned: the 16-byte tile kernel
+    declines it and the element-wise tile kernel (or its fallbacks) must
+    give the oracle's result."""
+    import torch
+    for (T, a, B) in ((9, 32, 11), (5, 11, 32), (3, 64, 700), (2, 16, 3)):
+        if a * B * e > 112 * 1024:
+            continue
+        n = T * a * B
+        src = O.random_bits(n, e, T + a + B + 7)
+        raw = torch.zeros(n * e + 64, dtype=torch.uint8, device="cuda")
+        view = raw[e:e + n * e]
+        view.copy_(torch.from_numpy(src.view(np.uint8).copy()).cuda())
+        assert view.data_ptr() % 16 != 0
+        assert not L.lib().lm_transpose_010_bs(None, view.data_ptr(), e, T, a,
+                                               B, None), L.last_error()
+        torch.cuda.synchronize()
+        got = view.cpu().numpy().view(O.DTYPES[e])
+        assert np.array_equal(got, O.t010(src, T, a, B)), (T, a, B, e)
