@@ -331,9 +331,6 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
     if (sp.feasible && status) {
       Scratch sc;
       if (get_scratch(sc, stash_scratch_bytes(sp), s)) return true;
-      cudaError_t ze = cudaMemsetAsync((char *)sc.p + stash_zero_offset(sp), 0,
-                                       stash_zero_bytes(sp), s);
-      if (ze != cudaSuccess) return cuda_fail(ze, "scratch clear");
       return check_launch(launch_stash100(s, buf, e, a, B, (uint32_t)b, sp,
                                           sc.p, status, wait_timeout_ns()),
                           "stash launch");

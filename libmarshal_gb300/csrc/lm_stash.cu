@@ -46,6 +46,7 @@ struct StashArgs {
   char *stash;
   const uint64_t *roff;  // byte offset of each row's stash suffix, A+1
   uint32_t *progress;    // one counter per row chunk
+  uint32_t progress_words;  // cleared by K1 before the wave starts
   uint32_t *status;
   uint64_t A, B;         // rows, columns (units)
   uint32_t b;            // elements per unit
@@ -177,6 +178,10 @@ constexpr int kSaveThreads = 256;
 
 __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
   const uint32_t lane = threadIdx.x & 31;
+  // the wave's progress counters start at zero (K2 runs after K1)
+  for (uint32_t x = blockIdx.x * kSaveThreads + threadIdx.x;
+       x < g.progress_words; x += gridDim.x * kSaveThreads)
+    g.progress[x] = 0u;
   const uint64_t gw = ((uint64_t)blockIdx.x * kSaveThreads + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * kSaveThreads) >> 5;
   const uint64_t U = (uint64_t)g.b * g.e;
@@ -822,6 +827,7 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   g.roff = reinterpret_cast<const uint64_t *>(sc + off);
   off += align((size_t)(A + 1) * 8);
   g.progress = reinterpret_cast<uint32_t *>(sc + off);
+  g.progress_words = (uint32_t)(stash_zero_bytes(p) / 4);
   g.status = status;
   g.A = A;
   g.B = B;
