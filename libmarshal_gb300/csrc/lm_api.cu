@@ -327,6 +327,13 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
   if (want_stash) {
     // 100 on small units: the 3 x payload streaming plan (lm_stash.cu).
     StashPlan sp = T == 1 ? plan_stash(a, B, (uint32_t)b, e) : StashPlan();
+    // very tall matrices leave each CTA short strips (a step's rows x strip
+    // must fit shared memory); below 384-byte strips the staged form moves
+    // units of 4 bytes and more faster (fp64 32768 x 16000: 3.06 TB/s by
+    // the stash with 256-byte strips, 3.24 TB/s staged)
+    if (m == Method::Auto && sp.feasible && U >= 4 && sp.g * U < 384 &&
+        staged0100_applies(T, a, B, b, e))
+      sp = StashPlan();
     uint32_t *status = sp.feasible ? device_status_word() : nullptr;
     if (sp.feasible && status) {
       Scratch sc;

@@ -230,7 +230,7 @@ constexpr int kCheckerWarp = kProducerWarps + 1;
 constexpr int kWriterWarps = kWaveThreads / 32 - kProducerWarps - 2;
 constexpr uint32_t kCheckAhead = 4;  // steps whose chunks the checker prefetches
 constexpr int kMaxRowBlocks = 4;  // rows per chunk <= 128
-constexpr uint32_t kStashMargin = 3;
+constexpr uint32_t kStashMargin = 2;
 constexpr uint32_t kMaxChunks = 1024;  // CTAs of the wave (co-resident)
 constexpr uint32_t kProgStride = 32;   // one 128-byte line per progress word
 // LM_STASH_TRACE slots per (chunk, step): 0 gather issued, 1 published,
