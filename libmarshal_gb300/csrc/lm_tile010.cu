@@ -43,48 +43,59 @@ struct T010Args {
   uint32_t R, P;     // row bytes (B*e); staged row pitch (form B)
   uint32_t tile_bytes;
   uint32_t stage;    // shared bytes of one input stage
+  uint32_t V;        // form A: output vector bytes (16, 8 or 4)
+  uint32_t form_b;   // 1: form B
   FastDiv div_B;     // form A: output vectors -> (column, row block)
-  FastDiv div_NA;    // form A: a*e/16 vectors per output row
+  FastDiv div_NA;    // form A: a*e/V vectors per output row
   FastDiv div_a;     // form B: staged row -> (tile, row)
   FastDiv div_NC;    // form B: R/16 pieces per input row
   FastDiv div_rows;  // form B: k*a rows of a full chunk
 };
 
-// 16/E elements at p, p + R, p + 2R, ... packed into one 16-byte vector.
+// V/E elements at p, p + R, p + 2R, ... packed into one V-byte vector
+// (element 0 in the lowest bytes).
+template <int E, int V> struct Vout;
+template <int E> struct Vout<E, 16> { using T = uint4; };
+template <int E> struct Vout<E, 8> { using T = uint2; };
+template <int E> struct Vout<E, 4> { using T = uint32_t; };
+
 template <int E>
-__device__ __forceinline__ uint4 gather_column(const unsigned char *p,
-                                               uint32_t R) {
-  uint4 v;
+__device__ __forceinline__ uint32_t gather_word(const unsigned char *p,
+                                                uint32_t R) {
+  // one 32-bit word: 4/E elements of a column
   if (E == 1) {
-    uint32_t w[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const uint32_t x0 = p[(4 * q + 0) * R], x1 = p[(4 * q + 1) * R];
-      const uint32_t x2 = p[(4 * q + 2) * R], x3 = p[(4 * q + 3) * R];
-      w[q] = __byte_perm(__byte_perm(x0, x1, 0x0040), __byte_perm(x2, x3, 0x0040),
-                         0x5410);
-    }
-    v = make_uint4(w[0], w[1], w[2], w[3]);
+    const uint32_t x0 = p[0], x1 = p[R], x2 = p[2 * R], x3 = p[3 * R];
+    return __byte_perm(__byte_perm(x0, x1, 0x0040), __byte_perm(x2, x3, 0x0040),
+                       0x5410);
   } else if (E == 2) {
     const unsigned short *s = reinterpret_cast<const unsigned short *>(p);
-    const uint32_t h = R / 2;
-    uint32_t w[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      w[q] = __byte_perm((uint32_t)s[(2 * q) * h], (uint32_t)s[(2 * q + 1) * h],
-                         0x5410);
-    v = make_uint4(w[0], w[1], w[2], w[3]);
-  } else if (E == 4) {
-    v.x = *reinterpret_cast<const uint32_t *>(p);
-    v.y = *reinterpret_cast<const uint32_t *>(p + R);
-    v.z = *reinterpret_cast<const uint32_t *>(p + 2 * R);
-    v.w = *reinterpret_cast<const uint32_t *>(p + 3 * R);
+    return __byte_perm((uint32_t)s[0], (uint32_t)s[R / 2], 0x5410);
   } else {
-    const uint2 lo = *reinterpret_cast<const uint2 *>(p);
-    const uint2 hi = *reinterpret_cast<const uint2 *>(p + R);
-    v = make_uint4(lo.x, lo.y, hi.x, hi.y);
+    return *reinterpret_cast<const uint32_t *>(p);
   }
-  return v;
+}
+
+template <int E, int V>
+__device__ __forceinline__ typename Vout<E, V>::T gather_column(
+    const unsigned char *p, uint32_t R) {
+  constexpr uint32_t RW = E >= 4 ? 1 : 4 / E;  // rows per 32-bit word
+  if constexpr (E == 8) {
+    const uint2 lo = *reinterpret_cast<const uint2 *>(p);
+    if constexpr (V == 16) {
+      const uint2 hi = *reinterpret_cast<const uint2 *>(p + R);
+      return make_uint4(lo.x, lo.y, hi.x, hi.y);
+    } else {
+      return lo;
+    }
+  } else if constexpr (V == 16) {
+    return make_uint4(gather_word<E>(p, R), gather_word<E>(p + RW * R, R),
+                      gather_word<E>(p + 2 * RW * R, R),
+                      gather_word<E>(p + 3 * RW * R, R));
+  } else if constexpr (V == 8) {
+    return make_uint2(gather_word<E>(p, R), gather_word<E>(p + RW * R, R));
+  } else {
+    return gather_word<E>(p, R);
+  }
 }
 
 // All threads: 16-byte cp.async copies of chunk c into `buf` (rows at pitch
@@ -93,8 +104,17 @@ template <bool PAD>
 __device__ __forceinline__ void t010_issue(const T010Args &g, uint64_t c,
                                            unsigned char *buf) {
   const uint32_t nt = (uint32_t)min64(g.k, g.T - c * g.k);
-  const uint32_t nv = nt * (g.tile_bytes / 16);
   const char *src = g.base + c * g.k * (uint64_t)g.tile_bytes;
+  uint32_t nv = nt * (g.tile_bytes / 16);
+  if (!PAD) {
+    // the 16-byte aligned superset of the chunk (whole vectors when the
+    // tiles are; else up to 15 bytes more at each end)
+    const uintptr_t s0 = (uintptr_t)src & ~(uintptr_t)15;
+    const uintptr_t s1 = ((uintptr_t)src + (uint64_t)nt * g.tile_bytes + 15) &
+                         ~(uintptr_t)15;
+    nv = (uint32_t)((s1 - s0) / 16);
+    src = reinterpret_cast<const char *>(s0);
+  }
   for (uint32_t v = threadIdx.x; v < nv; v += kT010Threads) {
     uint32_t off = v * 16;
     if (PAD) {
@@ -106,10 +126,11 @@ __device__ __forceinline__ void t010_issue(const T010Args &g, uint64_t c,
   cp_async_commit();
 }
 
-template <int E, bool FORM_B>
+template <int E, int VA, bool FORM_B>
 __global__ void __launch_bounds__(kT010Threads) k_tile010(T010Args g) {
   using T = typename Elem<E>::T;
   constexpr uint32_t VE = 16 / E;
+  constexpr uint32_t VEA = VA / E;  // form A: elements per output vector
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *img = smem + 2 * (size_t)g.stage;  // form B output image
   if (blockIdx.x >= g.nchunks) return;
@@ -129,7 +150,9 @@ __global__ void __launch_bounds__(kT010Threads) k_tile010(T010Args g) {
     const uint32_t nt = (uint32_t)min64(g.k, g.T - c * g.k);
     char *dst = g.base + c * g.k * (uint64_t)g.tile_bytes;
     if (!FORM_B) {
-      const uint32_t NA = g.a / VE;
+      using VT = typename Vout<E, VA>::T;
+      const unsigned char *c0 = cur + ((uintptr_t)dst & 15);  // chunk start
+      const uint32_t NA = g.a / VEA;
       const uint32_t nvec = nt * g.B * NA;
       const uint32_t orow = g.a * E;  // output row bytes
       for (uint32_t x = threadIdx.x; x < nvec; x += kT010Threads) {
@@ -138,8 +161,8 @@ __global__ void __launch_bounds__(kT010Threads) k_tile010(T010Args g) {
         const uint32_t t = fdiv(q, g.div_NA);
         const uint32_t ib = q - t * NA;
         const uint32_t tb = t * g.tile_bytes;
-        const uint4 v = gather_column<E>(cur + tb + ib * VE * g.R + jj * E, g.R);
-        __stcg(reinterpret_cast<uint4 *>(dst + tb + jj * orow + ib * 16), v);
+        const VT v = gather_column<E, VA>(c0 + tb + ib * VEA * g.R + jj * E, g.R);
+        *reinterpret_cast<VT *>(dst + tb + jj * orow + ib * VA) = v;
       }
     } else {
       const uint32_t rows = nt * g.a;
@@ -180,8 +203,15 @@ static bool t010_plan(const void *buf, int e, uint64_t T, uint64_t a,
   if (T == 0 || a < 2 || B < 2 || ((uintptr_t)buf & 15)) return false;
   const uint64_t tile = a * B * (uint64_t)e;
   if (tile > kT010MaxTile) return false;
-  const bool form_a = (a * e) % 16 == 0;  // form A when both apply
-  if (!form_a && (B * e) % 16 != 0) return false;
+  // form A when both apply; form A also with 8- or 4-byte output vectors
+  // when the output rows are whole such vectors (and a vector holds two
+  // elements or more)
+  uint32_t V = 0;
+  for (uint32_t v : {16u, 8u, 4u})
+    if (!V && (a * e) % v == 0 && (uint64_t)e < v) V = v;
+  const bool form_b = !(V == 16) && (B * e) % 16 == 0;
+  if (!form_b && !V) return false;
+  const bool form_a = !form_b;
   g->base = reinterpret_cast<char *>(const_cast<void *>(buf));
   g->T = T;
   g->a = (uint32_t)a;
@@ -197,12 +227,14 @@ static bool t010_plan(const void *buf, int e, uint64_t T, uint64_t a,
   g->nchunks = (T + g->k - 1) / g->k;
   g->P = g->R;
   if (!form_a && ((g->P / 16) & 1) == 0) g->P += 16;  // odd 16-byte words
-  g->stage = (uint32_t)(((form_a ? (uint64_t)g->k * tile
+  g->V = form_a ? V : 16u;
+  g->form_b = form_b ? 1u : 0u;
+  g->stage = (uint32_t)(((form_a ? (uint64_t)g->k * tile + 32
                                  : (uint64_t)g->k * a * g->P) + 127) / 128 * 128);
   *smem = 2 * (size_t)g->stage + (form_a ? 0 : (size_t)g->k * tile);
   if (*smem > (size_t)device_info().max_smem_optin) return false;
   g->div_B = make_fastdiv(g->B);
-  g->div_NA = make_fastdiv(std::max<uint32_t>(1, g->a * (uint32_t)e / 16));
+  g->div_NA = make_fastdiv(std::max<uint32_t>(1, g->a * (uint32_t)e / g->V));
   g->div_a = make_fastdiv(g->a);
   g->div_NC = make_fastdiv(std::max<uint32_t>(1, g->R / 16));
   g->div_rows = make_fastdiv(g->k * g->a);
@@ -216,10 +248,10 @@ bool tile010_applies(const void *buf, int e, uint64_t T, uint64_t a,
   return t010_plan(buf, e, T, a, B, &g, &smem);
 }
 
-template <int E, bool FORM_B>
+template <int E, int VA, bool FORM_B>
 static cudaError_t run_tile010(cudaStream_t s, const T010Args &g,
                                size_t smem) {
-  auto kern = k_tile010<E, FORM_B>;
+  auto kern = k_tile010<E, VA, FORM_B>;
   cudaError_t err = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
@@ -230,9 +262,9 @@ static cudaError_t run_tile010(cudaStream_t s, const T010Args &g,
   uint64_t blocks = (uint64_t)device_info().sms * std::max(occ, 1);
   if (g.nchunks < blocks) blocks = g.nchunks;
   if (getenv("LM_VERBOSE"))
-    fprintf(stderr, "tile010: form %c e=%d k=%u stage=%u smem=%zu occ=%d "
-            "blocks=%llu chunks=%llu\n", FORM_B ? 'B' : 'A', E, g.k, g.stage,
-            smem, occ, (unsigned long long)blocks,
+    fprintf(stderr, "tile010: form %c e=%d V=%d k=%u stage=%u smem=%zu occ=%d "
+            "blocks=%llu chunks=%llu\n", FORM_B ? 'B' : 'A', E, VA, g.k,
+            g.stage, smem, occ, (unsigned long long)blocks,
             (unsigned long long)g.nchunks);
   ProfScope ps(s, "tile010");
   kern<<<(unsigned)blocks, kT010Threads, smem, s>>>(g);
@@ -244,16 +276,25 @@ cudaError_t launch_tile010(cudaStream_t s, void *buf, int e, uint64_t T,
   T010Args g;
   size_t smem = 0;
   if (!t010_plan(buf, e, T, a, B, &g, &smem)) return cudaErrorInvalidValue;
-  const bool form_b = (a * (uint32_t)e) % 16 != 0;
-  switch (e) {
-    case 1: return form_b ? run_tile010<1, true>(s, g, smem)
-                          : run_tile010<1, false>(s, g, smem);
-    case 2: return form_b ? run_tile010<2, true>(s, g, smem)
-                          : run_tile010<2, false>(s, g, smem);
-    case 4: return form_b ? run_tile010<4, true>(s, g, smem)
-                          : run_tile010<4, false>(s, g, smem);
-    default: return form_b ? run_tile010<8, true>(s, g, smem)
-                           : run_tile010<8, false>(s, g, smem);
+  if (g.form_b) {
+    switch (e) {
+      case 1: return run_tile010<1, 16, true>(s, g, smem);
+      case 2: return run_tile010<2, 16, true>(s, g, smem);
+      case 4: return run_tile010<4, 16, true>(s, g, smem);
+      default: return run_tile010<8, 16, true>(s, g, smem);
+    }
+  }
+  switch (e * 100 + g.V) {
+    case 116: return run_tile010<1, 16, false>(s, g, smem);
+    case 108: return run_tile010<1, 8, false>(s, g, smem);
+    case 104: return run_tile010<1, 4, false>(s, g, smem);
+    case 216: return run_tile010<2, 16, false>(s, g, smem);
+    case 208: return run_tile010<2, 8, false>(s, g, smem);
+    case 204: return run_tile010<2, 4, false>(s, g, smem);
+    case 416: return run_tile010<4, 16, false>(s, g, smem);
+    case 408: return run_tile010<4, 8, false>(s, g, smem);
+    case 816: return run_tile010<8, 16, false>(s, g, smem);
+    default: return cudaErrorInvalidValue;
   }
 }
 

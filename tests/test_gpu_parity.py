@@ -458,14 +458,18 @@ TILE010_SHAPES = [
     (1, 64, 200), (2049, 32, 7), (777, 13, 64), (3, 512, 16), (5, 16, 512),
     (4, 64, 700), (3, 700, 64), (2, 1000, 32), (3, 48, 1000),
     (3, 32, 1700), (2, 1700, 32), (3, 16, 7000),
+    # output rows of whole 8- or 4-byte vectors only (chunks not 16-byte
+    # aligned): form A with narrower vectors
+    (1296, 100, 100), (7, 12, 5), (5, 24, 7), (9, 6, 13), (333, 20, 9),
 ]
 
 
 @pytest.mark.parametrize("e", [1, 2, 4, 8])
 def test_tile010_forms(L, e):
-    """010 on 16-byte aligned buffers through the 16-byte tile kernel (both
-    forms, ragged last chunk, one-tile and many-tile cases) and with it
-    switched off (the element-wise tile kernel), against the oracle."""
+    """010 on 16-byte aligned buffers through the vector tile kernel (both
+    forms, 16-, 8- and 4-byte output vectors, ragged last chunk, one-tile
+    and many-tile cases) and with it switched off (the element-wise tile
+    kernel), against the oracle."""
     import torch
     for (T, a, B) in TILE010_SHAPES:
         if a * B * e > 112 * 1024:
