@@ -13,6 +13,7 @@
 // the device's stream-ordered memory pool (cudaMallocAsync / cudaFreeAsync on
 // the caller's stream), so concurrent calls on different streams never share
 // it and repeated calls reuse pooled memory instead of allocating.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -80,16 +81,16 @@ static bool cuda_fail(cudaError_t e, const char *what) {
 // ---- scratch ----------------------------------------------------------------
 
 void pool_keep_memory() {
-  static bool done[64] = {false};
+  static std::atomic<bool> done[64];
   int dev = 0;
   cudaGetDevice(&dev);
-  if (done[dev & 63]) return;
+  if (done[dev & 63].load(std::memory_order_acquire)) return;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
     uint64_t thr = ~0ull;  // keep freed blocks pooled between calls
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
-  done[dev & 63] = true;
+  done[dev & 63].store(true, std::memory_order_release);
 }
 
 struct Scratch {
