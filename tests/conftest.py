@@ -12,7 +12,7 @@ def pytest_configure(config):
     config.addinivalue_line(
         "markers", "gpu: needs a CUDA GPU (GB300); parity tests proper")
     config.addinivalue_line(
-        "markers", "slow: large shapes (full BASELINE sizes)")
+        "markers", "slow: large shapes (the full benchmark sizes)")
 
 
 @pytest.fixture(scope="session")

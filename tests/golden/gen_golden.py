@@ -48,7 +48,7 @@ def make_input(kind: str, n: int, e: int, seed: int) -> np.ndarray:
 
 def aos_cases():
     c = []
-    # BASELINE cfg1: AoS [65536][7] fp32, ASTA tile 32, and the inverse.
+    # AoS [65536][7] fp32 to ASTA with tile 32, and the inverse.
     c.append(dict(h=65536, w=7, t=32, e=4, fill="random", seed=0, tag="cfg1"))
     c.append(dict(h=2048 * 7, w=32, t=7, e=4, fill="random", seed=0,
                   tag="cfg1-inverse-on-random"))
@@ -102,7 +102,7 @@ def soa_cases():
 
 def full_cases():
     c = []
-    # BASELINE cfg2 and the PPoPP'14 sizes (cl_unittest.cc:386-387).
+    # the 7200x1800 staged transposition and the PPoPP'14 sizes (cl_unittest.cc:386-387).
     for e in (1, 2, 4, 8):
         c.append(dict(M=7200, N=1800, e=e, fill="index", seed=0, tag="cfg2"))
     for (M, N) in ((5100, 2500), (4000, 3200), (3300, 3900), (2500, 5100),

@@ -151,7 +151,7 @@ def test_full_transpose_planner_golden(L, c):
 @pytest.mark.parametrize("stages", [2, 22, 3, 32, 4, 0])
 @pytest.mark.parametrize("variant", [1, 2])
 def test_cfg2_every_stage_and_variant(L, e, stages, variant):
-    # BASELINE 7200x1800 with index fill; a=100, A=72, b=100, B=18
+    # the 7200x1800 staged transposition with index fill; a=100, A=72, b=100, B=18
     c = [c for c in GOLDEN["full"] if c["tag"] == "cfg2" and c["e"] == e][0]
     src = make(c, 7200 * 1800)
     d = to_dev(src)
@@ -416,7 +416,7 @@ def _full_size_100(L, A, B, e, seed):
 
 
 def test_headline_full_size_fp32(L):
-    # BASELINE headline: in-place 100 of the fp32 16384 x 12289 matrix
+    # the headline workload: in-place 100 of the fp32 16384 x 12289 matrix
     _full_size_100(L, 16384, 12289, 4, 2024)
 
 

@@ -84,7 +84,7 @@ def test_factorize_and_tile_options_match_reference():
 
 
 def test_alg5_alg3_baseline_shapes():
-    # BASELINE 7200x1800: a=100, A=72, b=100, B=18, no padding, stage 3
+    # the 7200x1800 staged transposition: a=100, A=72, b=100, B=18, no padding, stage 3
     assert O.alg5(7200, 1800) == (72, 100, 18, 100, 0, 0)
     assert O.alg3(72, 100, 18, 100) == 3
     # 16384x12289 (12289 prime): pads w to 12291 = 3*17*241 -> b=51, stage 32
