@@ -578,7 +578,8 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
   // Strip per step: the largest (1024 bytes down to 128, in steps of 128)
   // that keeps a CTA's step at most kStepBytes and three ring stages within
   // shared memory, two CTAs per SM first.  Longer steps amortise each step's
-  // handshakes; the sweep on both headline directions and fp64 peaked near
+  // handshakes; the sweep on both directions of the fp32 16384 x 12289
+  // transposition and on fp64 peaked near
   // 32-40 KB per step.  LM_STASH_STRIP / LM_STASH_PER_SM force a choice.
   const char *es = getenv("LM_STASH_STRIP");
   const char *ep = getenv("LM_STASH_PER_SM");
