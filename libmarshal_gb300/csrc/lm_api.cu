@@ -80,6 +80,33 @@ static bool cuda_fail(cudaError_t e, const char *what) {
 
 // ---- scratch ----------------------------------------------------------------
 
+int prepare_launch(const void *kern, LaunchCache &c, size_t smem, int threads,
+                   cudaError_t *err) {
+  *err = cudaSuccess;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int d = dev & 7;
+  const int need = (int)smem + 1;
+  if (need > 48 * 1024 + 1 && c.smem_set[d].load(std::memory_order_acquire) < need) {
+    if ((*err = cudaFuncSetAttribute(kern,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem)) != cudaSuccess)
+      return 0;
+    int cur = c.smem_set[d].load();
+    while (cur < need && !c.smem_set[d].compare_exchange_weak(cur, need)) {
+    }
+  }
+  const uint64_t key = c.occ_key[d].load(std::memory_order_acquire);
+  if (key && (key >> 16) == (uint64_t)smem) return (int)(key & 0xffff);
+  int occ = 0;
+  if ((*err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads,
+                                                            smem)) != cudaSuccess)
+    return 0;
+  c.occ_key[d].store(((uint64_t)smem << 16) | (uint64_t)(occ & 0xffff),
+                     std::memory_order_release);
+  return occ;
+}
+
 void pool_keep_memory() {
   static std::atomic<bool> done[64];
   int dev = 0;

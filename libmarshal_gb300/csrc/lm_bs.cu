@@ -318,13 +318,11 @@ template <int E, bool CLUSTER>
 static cudaError_t run_bs(cudaStream_t s, const BsArgs &g, const BsPlan &p) {
   auto kern = CLUSTER ? k_bs0100_band<E> : k_bs0100<E>;
   const DeviceInfo &di = device_info();
-  cudaError_t err = cudaFuncSetAttribute(
-      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
-  if (err != cudaSuccess) return err;
+  cudaError_t err = cudaSuccess;
   if (!CLUSTER) {
-    int occ = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBsThreads,
-                                                        p.smem_bytes);
+    static LaunchCache cache;
+    const int occ = prepare_launch((const void *)kern, cache, p.smem_bytes,
+                                   kBsThreads, &err);
     if (err != cudaSuccess) return err;
     uint64_t blocks = (uint64_t)di.sms * std::max(occ, 1);
     if (g.nchunks < blocks) blocks = g.nchunks;
@@ -336,6 +334,9 @@ static cudaError_t run_bs(cudaStream_t s, const BsArgs &g, const BsPlan &p) {
     kern<<<(unsigned)blocks, kBsThreads, p.smem_bytes, s>>>(g);
     return cudaGetLastError();
   }
+  err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)p.smem_bytes);
+  if (err != cudaSuccess) return err;
   if (p.cluster > 8) {
     err = cudaFuncSetAttribute(kern,
                                cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

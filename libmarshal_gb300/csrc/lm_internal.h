@@ -3,6 +3,7 @@
 // (scratch is passed in) and returns cudaSuccess or the launch error.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -56,6 +57,20 @@ BsPlan plan_bs0100(uint64_t T, uint32_t a, uint32_t B, uint32_t b, int e,
 cudaError_t launch_bs0100(cudaStream_t s, void *buf, int e, uint64_t T,
                           uint32_t a, uint32_t B, uint32_t b,
                           const BsPlan &plan);
+
+// ---- launch preparation cache ---------------------------------------------
+// A kernel's dynamic shared-memory limit is raised only when a launch needs
+// more than any before it on this device, and its occupancy is remembered
+// for the last size asked: small conversions are bound by host time per
+// call, and these driver queries cost about as much as the launch itself.
+struct LaunchCache {
+  std::atomic<int> smem_set[8];       // per device: largest limit set (+1)
+  std::atomic<uint64_t> occ_key[8];   // per device: (smem << 16) | occupancy
+};
+// Sets the attribute if needed and returns the CTAs per SM for `threads`
+// threads and `smem` dynamic bytes (0 on error, with *err set).
+int prepare_launch(const void *kern, LaunchCache &c, size_t smem, int threads,
+                   cudaError_t *err);
 
 // ---- planner thresholds (the per-op planner and the batch executor) ------
 // Measured on GB300 with 256 MB matrices: the staged form (4 x payload

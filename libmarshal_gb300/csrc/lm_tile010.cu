@@ -252,12 +252,10 @@ template <int E, int VA, bool FORM_B>
 static cudaError_t run_tile010(cudaStream_t s, const T010Args &g,
                                size_t smem) {
   auto kern = k_tile010<E, VA, FORM_B>;
-  cudaError_t err = cudaFuncSetAttribute(
-      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  int occ = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kT010Threads,
-                                                      smem);
+  static LaunchCache cache;
+  cudaError_t err = cudaSuccess;
+  const int occ = prepare_launch((const void *)kern, cache, smem, kT010Threads,
+                                 &err);
   if (err != cudaSuccess) return err;
   uint64_t blocks = (uint64_t)device_info().sms * std::max(occ, 1);
   if (g.nchunks < blocks) blocks = g.nchunks;
