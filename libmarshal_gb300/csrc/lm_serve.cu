@@ -49,7 +49,7 @@ constexpr int kSlots = 2;
 constexpr uint64_t kLaneLimit[kLanes - 1] = {2ull << 20, 64ull << 20};
 // batch limits per lane: requests and payload bytes; staging arena of each
 // slot's batch handle
-constexpr size_t kLaneMaxReqs[kLanes] = {4096, 256, 8};
+constexpr size_t kLaneMaxReqs[kLanes] = {4096, 256, 4};
 constexpr uint64_t kLaneMaxBytes[kLanes] = {1ull << 30, 4ull << 30, 8ull << 30};
 constexpr uint64_t kLaneArena[kLanes] = {1ull << 30, 2ull << 30, 4ull << 30};
 
