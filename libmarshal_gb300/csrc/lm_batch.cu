@@ -36,12 +36,18 @@ constexpr int kMaxWaves = 32;        // staged waves per batch
 constexpr int kCounterStride = 32;   // counters 128 bytes apart
 // small, big, one per cluster size, two per staged wave
 constexpr size_t kCounterBytes =
-    (size_t)(2 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
+    (size_t)(3 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
+constexpr int kT010Counter = 2 + kBandGroups + 2 * kMaxWaves;
 constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
 // jobs at least this large that the stash plan applies to skip the staged
 // form (the stash moves 3 x payload, the staged form 4 x)
 constexpr uint64_t kStashPreferBytes = 64ull << 20;
-constexpr int kSideStreams = 5;      // streams of the large jobs and groups
+constexpr int kSideStreams = 6;      // streams of the large jobs and groups
+// small jobs of one-element units whose output rows are whole 16-byte
+// vectors (a*e a multiple of 16, aligned buffer) with tiles of at most
+// this size go to the batched 16-byte tile kernel, in items of about
+// this size
+constexpr uint32_t kT010BatchBytes = 16 * 1024;
 // jobs at least this large that the 16-byte tile kernel applies to run as
 // launches of their own
 constexpr uint64_t kTile010PreferBytes = 2ull << 20;
@@ -64,6 +70,7 @@ struct BJob {
   // staged blocks)
   uint32_t ng8;
   FastDiv div_ng8;
+  FastDiv div_na;  // a*e/16: 16-byte vectors per output row (tile kernel)
 };
 
 struct BItem {
@@ -373,6 +380,86 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_small(BatchArgs g) {
   }
 }
 
+
+// Batched form of the 16-byte tile kernel (lm_tile010.cu, form A): items
+// of whole tiles of jobs with one-element units whose output rows are whole
+// 16-byte vectors, claimed from a counter; the 16-byte cp.async copies of
+// the next item land while the current one is written.  Each output vector
+// is built from 16/e rows of one staged column.
+template <int E>
+__device__ __forceinline__ void t010_item_store(const BJob &j, const BItem &it,
+                                                const unsigned char *cur) {
+  constexpr uint32_t VE = 16 / E;
+  const uint32_t B = j.row_elems, R = B * E, NA = j.a / VE;
+  const uint32_t tb_bytes = j.tile_elems * E;
+  char *dst = j.base + it.tile0 * (uint64_t)tb_bytes;
+  const uint32_t nvec = it.ntiles * B * NA;
+  const uint32_t orow = j.a * E;
+  for (uint32_t x = threadIdx.x; x < nvec; x += kBatchThreads) {
+    const uint32_t q = fdiv(x, j.div_row);
+    const uint32_t jj = x - q * B;
+    const uint32_t t = fdiv(q, j.div_na);
+    const uint32_t ib = q - t * NA;
+    const uint32_t tb = t * tb_bytes;
+    const uint4 v = gather_column<E, 16>(cur + tb + ib * VE * R + jj * E, R);
+    __stcg(reinterpret_cast<uint4 *>(dst + tb + jj * orow + ib * 16), v);
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads) k_batch_t010(BatchArgs g) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint32_t s_item[2];
+  __shared__ __align__(16) BJob s_jobs[2];
+  __shared__ __align__(16) BItem s_it[2];
+  const uint32_t warp = threadIdx.x >> 5;
+  auto claim = [&](int sl) -> bool {
+    if (threadIdx.x == 0) s_item[sl] = atomicAdd(g.counter, 1u);
+    __syncthreads();
+    const uint32_t k = s_item[sl];
+    if (k < g.nitems && warp == 0) {
+      const BItem it = g.items[k];
+      copy_job(&s_jobs[sl], &g.jobs[it.job]);
+      if ((threadIdx.x & 31) == 0) s_it[sl] = it;
+    }
+    __syncthreads();
+    return k < g.nitems;
+  };
+  auto issue = [&](int sl) {
+    const BJob &j = s_jobs[sl];
+    const BItem &it = s_it[sl];
+    const uint64_t tbytes = (uint64_t)j.tile_elems * j.e;
+    const char *src = j.base + it.tile0 * tbytes;
+    const uint32_t nv = (uint32_t)(it.ntiles * tbytes / 16);
+    unsigned char *buf = smem + (size_t)sl * g.stage_bytes;
+    for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads)
+      cp_async16(buf + (size_t)v * 16, src + (uint64_t)v * 16);
+    cp_async_commit();
+  };
+  if (!claim(0)) return;
+  issue(0);
+  for (uint32_t n = 0;; ++n) {
+    const int st = n & 1, nx = st ^ 1;
+    // slot and stage nx were last read before the previous pass's barrier
+    const bool more = claim(nx);
+    if (more) {
+      issue(nx);
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_all();
+    }
+    __syncthreads();  // item n staged by every thread's copies
+    const BJob &j = s_jobs[st];
+    const unsigned char *cur = smem + (size_t)st * g.stage_bytes;
+    switch (j.e) {
+      case 1: t010_item_store<1>(j, s_it[st], cur); break;
+      case 2: t010_item_store<2>(j, s_it[st], cur); break;
+      case 4: t010_item_store<4>(j, s_it[st], cur); break;
+      default: t010_item_store<8>(j, s_it[st], cur); break;
+    }
+    __syncthreads();  // stage st and slot st free
+    if (!more) break;
+  }
+}
 
 // Writes nrows x ncols staged elements (b == 1) transposed: output row jj
 // (stride `ostride` elements from `dst`) gets staged column jj.  A warp
@@ -1043,6 +1130,7 @@ bool op_as_0100(int op, long long d0, long long d1, long long d2, long long d3,
 struct lm_batch_st {
   std::vector<lm::BJob> jobs;
   std::vector<lm::BItem> small, big;
+  std::vector<lm::BItem> t010;  // items of the batched 16-byte tile kernel
   std::vector<lm::BItem> band[lm::kBandGroups];  // cluster of 2 << g CTAs
   size_t band_smem[lm::kBandGroups] = {};
   // staged waves: gather items, copy-back items, shared memory of the gather
@@ -1188,6 +1276,7 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.band = 0;
   j.ng8 = (uint32_t)((nz.a + 7) / 8);
   j.div_ng8 = make_fastdiv(j.ng8);
+  j.div_na = make_fastdiv((uint32_t)std::max<uint64_t>(1, nz.a * nz.e / 16));
   j.scratch = nullptr;
   j.S = j.Sj = j.nJ = j.nIJ = j.nv16 = 0;
   j.bytes = 0;
@@ -1270,6 +1359,7 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
       ((size_t)di.max_smem_per_sm / 2 - 1024 - band_static) / 2 / 128 * 128;
   bt->jobs.clear();
   bt->small.clear();
+  bt->t010.clear();
   bt->big.clear();
   for (int gi = 0; gi < kBandGroups; ++gi) {
     bt->band[gi].clear();
@@ -1452,19 +1542,26 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
     fill_job(j, jb, nz, pitch);
     const uint32_t jid = (uint32_t)bt->jobs.size();
     bt->jobs.push_back(j);
-    uint64_t k_t = std::max<uint64_t>(1, kSmallItem / tile_smem);
+    const uint64_t tile_bytes = tile_elems * (uint64_t)e;
+    // whole-vector output rows on an aligned buffer: the batched 16-byte
+    // tile kernel (items of about kT010BatchBytes), else the general one
+    const bool vec = nz.b == 1 && ((uintptr_t)jb.buf & 15) == 0 &&
+                     (nz.a * (uint64_t)e) % 16 == 0 &&
+                     tile_bytes <= kT010BatchBytes && !getenv("LM_NO_TILE010");
+    uint64_t k_t = vec ? std::max<uint64_t>(1, kT010BatchBytes / tile_bytes)
+                       : std::max<uint64_t>(1, kSmallItem / tile_smem);
     while (k_t > 1 && k_t * tile_elems >= 0xffffffffull) --k_t;
     for (uint64_t t0 = 0; t0 < nz.T; t0 += k_t) {
       BItem it;
       it.job = jid;
       it.tile0 = t0;
       it.ntiles = (uint32_t)std::min<uint64_t>(k_t, nz.T - t0);
-      bt->small.push_back(it);
+      (vec ? bt->t010 : bt->small).push_back(it);
     }
     bt->stats.small_jobs += 1;
     bt->stats.small_bytes += bytes;
   }
-  bt->stats.small_items = bt->small.size();
+  bt->stats.small_items = bt->small.size() + bt->t010.size();
   bt->stats.big_items = bt->big.size();
   for (int gi = 0; gi < kBandGroups; ++gi)
     bt->stats.band_items += bt->band[gi].size();
@@ -1665,6 +1762,32 @@ static bool launch_small(cudaStream_t s, const BJob *d_jobs,
   return false;
 }
 
+static bool launch_t010(cudaStream_t s, const BJob *d_jobs,
+                        const BItem *d_items, uint32_t nitems,
+                        uint32_t *counter) {
+  if (nitems == 0) return false;
+  const size_t smem = 2 * (size_t)kT010BatchBytes;
+  static LaunchCache cache;
+  cudaError_t err = cudaSuccess;
+  const int occ = prepare_launch((const void *)k_batch_t010, cache, smem,
+                                 kBatchThreads, &err);
+  if (err != cudaSuccess || occ < 1) return set_error("batch: tile kernel setup");
+  const DeviceInfo &di = device_info();
+  const uint32_t grid =
+      (uint32_t)std::min<uint64_t>((uint64_t)di.sms * occ, nitems);
+  BatchArgs g{};
+  g.jobs = d_jobs;
+  g.items = d_items;
+  g.nitems = nitems;
+  g.counter = counter;
+  g.status = nullptr;
+  g.stage_bytes = kT010BatchBytes;
+  ProfScope ps(s, "batch_tile010");
+  k_batch_t010<<<grid, kBatchThreads, smem, s>>>(g);
+  if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
+  return false;
+}
+
 static bool launch_items(cudaStream_t s, const BJob *d_jobs,
                          const BItem *d_items, uint32_t nitems,
                          uint32_t *counter, size_t smem) {
@@ -1693,7 +1816,7 @@ static bool launch_items(cudaStream_t s, const BJob *d_jobs,
 
 // Records the work of the planned batch on stream s.
 static size_t item_count(lm_batch_t bt) {
-  size_t n = bt->small.size() + bt->big.size();
+  size_t n = bt->small.size() + bt->big.size() + bt->t010.size();
   for (int gi = 0; gi < kBandGroups; ++gi) n += bt->band[gi].size();
   for (int w = 0; w < bt->nwaves; ++w)
     n += bt->wgather[w].size() + bt->wcopy[w].size();
@@ -1798,6 +1921,7 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
       put(bt->wgather[w]);
       put(bt->wcopy[w]);
     }
+    put(bt->t010);
   }
   if (nj && cudaMemcpyAsync(bt->d_jobs, h, nj * sizeof(BJob),
                             cudaMemcpyHostToDevice, s) != cudaSuccess)
@@ -1829,9 +1953,13 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
     off += bt->band[gi].size();
   }
   const size_t off_waves = off;
+  for (int w = 0; w < bt->nwaves; ++w)
+    off += bt->wgather[w].size() + bt->wcopy[w].size();
+  const size_t off_t010 = off;
   int nq = 0;
-  cudaStream_t q[1 + kBandGroups + 1];
-  int ngroups = (bt->nwaves > 0) + (!bt->small.empty() || !bt->big.empty());
+  cudaStream_t q[1 + kBandGroups + 2];
+  int ngroups = (bt->nwaves > 0) + (!bt->small.empty() || !bt->big.empty()) +
+                !bt->t010.empty();
   for (int gi = 0; gi < kBandGroups; ++gi) ngroups += !bt->band[gi].empty();
   if (ngroups > 1) {
     if (ensure_side(bt)) return true;
@@ -1884,6 +2012,13 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
                        (size_t)di.max_smem_optin - 1024))
         return true;
     }
+  }
+  if (!bt->t010.empty()) {
+    const cudaStream_t vs = next_stream();
+    if (launch_t010(vs, bt->d_jobs, bt->d_items + off_t010,
+                    (uint32_t)bt->t010.size(),
+                    bt->d_counters + kT010Counter * kCounterStride))
+      return true;
   }
   for (int k = 0; k < kSideStreams; ++k) {
     if (!((used >> k) & 1)) continue;

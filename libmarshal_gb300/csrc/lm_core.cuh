@@ -164,6 +164,52 @@ __device__ __forceinline__ void store_columns16(const unsigned char *buf,
   }
 }
 
+// V/E elements at p, p + R, p + 2R, ... packed into one V-byte vector
+// (element 0 in the lowest bytes).
+template <int E, int V> struct Vout;
+template <int E> struct Vout<E, 16> { using T = uint4; };
+template <int E> struct Vout<E, 8> { using T = uint2; };
+template <int E> struct Vout<E, 4> { using T = uint32_t; };
+
+template <int E>
+__device__ __forceinline__ uint32_t gather_word(const unsigned char *p,
+                                                uint32_t R) {
+  // one 32-bit word: 4/E elements of a column
+  if (E == 1) {
+    const uint32_t x0 = p[0], x1 = p[R], x2 = p[2 * R], x3 = p[3 * R];
+    return __byte_perm(__byte_perm(x0, x1, 0x0040), __byte_perm(x2, x3, 0x0040),
+                       0x5410);
+  } else if (E == 2) {
+    const unsigned short *s = reinterpret_cast<const unsigned short *>(p);
+    return __byte_perm((uint32_t)s[0], (uint32_t)s[R / 2], 0x5410);
+  } else {
+    return *reinterpret_cast<const uint32_t *>(p);
+  }
+}
+
+template <int E, int V>
+__device__ __forceinline__ typename Vout<E, V>::T gather_column(
+    const unsigned char *p, uint32_t R) {
+  constexpr uint32_t RW = E >= 4 ? 1 : 4 / E;  // rows per 32-bit word
+  if constexpr (E == 8) {
+    const uint2 lo = *reinterpret_cast<const uint2 *>(p);
+    if constexpr (V == 16) {
+      const uint2 hi = *reinterpret_cast<const uint2 *>(p + R);
+      return make_uint4(lo.x, lo.y, hi.x, hi.y);
+    } else {
+      return lo;
+    }
+  } else if constexpr (V == 16) {
+    return make_uint4(gather_word<E>(p, R), gather_word<E>(p + RW * R, R),
+                      gather_word<E>(p + 2 * RW * R, R),
+                      gather_word<E>(p + 3 * RW * R, R));
+  } else if constexpr (V == 8) {
+    return make_uint2(gather_word<E>(p, R), gather_word<E>(p + RW * R, R));
+  } else {
+    return gather_word<E>(p, R);
+  }
+}
+
 // Drops the 128-byte L2 line at p (128-byte aligned) without writing it
 // back: its contents become undefined.  For scratch that has been read for
 // the last time, so that dirty staging lines never reach DRAM.
