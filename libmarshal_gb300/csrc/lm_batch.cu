@@ -36,7 +36,7 @@ constexpr int kMaxWaves = 32;        // staged waves per batch
 constexpr int kCounterStride = 32;   // counters 128 bytes apart
 // small, big, one per cluster size, two per staged wave
 constexpr size_t kCounterBytes =
-    (size_t)(3 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
+    (size_t)(4 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
 constexpr int kT010Counter = 2 + kBandGroups + 2 * kMaxWaves;
 constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
 // jobs at least this large that the stash plan applies to skip the staged
@@ -1131,6 +1131,8 @@ struct lm_batch_st {
   std::vector<lm::BJob> jobs;
   std::vector<lm::BItem> small, big;
   std::vector<lm::BItem> t010;  // items of the batched 16-byte tile kernel
+  std::vector<lm::BItem> t010b;  // the same, one larger tile per item
+  size_t t010b_stage = 0;       // bytes of the largest such tile
   std::vector<lm::BItem> band[lm::kBandGroups];  // cluster of 2 << g CTAs
   size_t band_smem[lm::kBandGroups] = {};
   // staged waves: gather items, copy-back items, shared memory of the gather
@@ -1360,6 +1362,8 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
   bt->jobs.clear();
   bt->small.clear();
   bt->t010.clear();
+  bt->t010b.clear();
+  bt->t010b_stage = 0;
   bt->big.clear();
   for (int gi = 0; gi < kBandGroups; ++gi) {
     bt->band[gi].clear();
@@ -1428,6 +1432,31 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
       bt->large.push_back((uint32_t)k);
       bt->stats.large_jobs += 1;
       bt->stats.large_bytes += bytes;
+      continue;
+    }
+    // tiles above kT010BatchBytes up to 112 KB with whole-vector output rows
+    // on an aligned buffer: the batched 16-byte tile kernel, one tile per
+    // item (two stages of the largest tile)
+    if (nz.b == 1 && ((uintptr_t)jb.buf & 15) == 0 &&
+        (nz.a * (uint64_t)e) % 16 == 0 && tile_elems * e > kT010BatchBytes &&
+        tile_elems * e <= 112 * 1024 &&
+        2 * ((tile_elems * e + 127) / 128 * 128) <= max_tile &&
+        !getenv("LM_NO_TILE010")) {
+      BJob j;
+      fill_job(j, jb, nz, pitch);
+      const uint32_t jid = (uint32_t)bt->jobs.size();
+      bt->jobs.push_back(j);
+      for (uint64_t t0 = 0; t0 < nz.T; ++t0) {
+        BItem it;
+        it.job = jid;
+        it.tile0 = t0;
+        it.ntiles = 1;
+        bt->t010b.push_back(it);
+      }
+      bt->t010b_stage = std::max<size_t>(
+          bt->t010b_stage, (size_t)((tile_elems * e + 127) / 128 * 128));
+      bt->stats.small_jobs += 1;
+      bt->stats.small_bytes += bytes;
       continue;
     }
     if (tile_elems >= 0xffffffffull || tile_smem > kSmallItem) {
@@ -1561,7 +1590,7 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
     bt->stats.small_jobs += 1;
     bt->stats.small_bytes += bytes;
   }
-  bt->stats.small_items = bt->small.size() + bt->t010.size();
+  bt->stats.small_items = bt->small.size() + bt->t010.size() + bt->t010b.size();
   bt->stats.big_items = bt->big.size();
   for (int gi = 0; gi < kBandGroups; ++gi)
     bt->stats.band_items += bt->band[gi].size();
@@ -1764,9 +1793,9 @@ static bool launch_small(cudaStream_t s, const BJob *d_jobs,
 
 static bool launch_t010(cudaStream_t s, const BJob *d_jobs,
                         const BItem *d_items, uint32_t nitems,
-                        uint32_t *counter) {
+                        uint32_t *counter, uint32_t stage) {
   if (nitems == 0) return false;
-  const size_t smem = 2 * (size_t)kT010BatchBytes;
+  const size_t smem = 2 * (size_t)stage;
   static LaunchCache cache;
   cudaError_t err = cudaSuccess;
   const int occ = prepare_launch((const void *)k_batch_t010, cache, smem,
@@ -1781,7 +1810,7 @@ static bool launch_t010(cudaStream_t s, const BJob *d_jobs,
   g.nitems = nitems;
   g.counter = counter;
   g.status = nullptr;
-  g.stage_bytes = kT010BatchBytes;
+  g.stage_bytes = stage;
   ProfScope ps(s, "batch_tile010");
   k_batch_t010<<<grid, kBatchThreads, smem, s>>>(g);
   if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
@@ -1816,7 +1845,8 @@ static bool launch_items(cudaStream_t s, const BJob *d_jobs,
 
 // Records the work of the planned batch on stream s.
 static size_t item_count(lm_batch_t bt) {
-  size_t n = bt->small.size() + bt->big.size() + bt->t010.size();
+  size_t n = bt->small.size() + bt->big.size() + bt->t010.size() +
+             bt->t010b.size();
   for (int gi = 0; gi < kBandGroups; ++gi) n += bt->band[gi].size();
   for (int w = 0; w < bt->nwaves; ++w)
     n += bt->wgather[w].size() + bt->wcopy[w].size();
@@ -1922,6 +1952,7 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
       put(bt->wcopy[w]);
     }
     put(bt->t010);
+    put(bt->t010b);
   }
   if (nj && cudaMemcpyAsync(bt->d_jobs, h, nj * sizeof(BJob),
                             cudaMemcpyHostToDevice, s) != cudaSuccess)
@@ -1959,7 +1990,7 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   int nq = 0;
   cudaStream_t q[1 + kBandGroups + 2];
   int ngroups = (bt->nwaves > 0) + (!bt->small.empty() || !bt->big.empty()) +
-                !bt->t010.empty();
+                (!bt->t010.empty() || !bt->t010b.empty());
   for (int gi = 0; gi < kBandGroups; ++gi) ngroups += !bt->band[gi].empty();
   if (ngroups > 1) {
     if (ensure_side(bt)) return true;
@@ -2013,11 +2044,17 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
         return true;
     }
   }
-  if (!bt->t010.empty()) {
+  if (!bt->t010.empty() || !bt->t010b.empty()) {
     const cudaStream_t vs = next_stream();
     if (launch_t010(vs, bt->d_jobs, bt->d_items + off_t010,
                     (uint32_t)bt->t010.size(),
-                    bt->d_counters + kT010Counter * kCounterStride))
+                    bt->d_counters + kT010Counter * kCounterStride,
+                    kT010BatchBytes))
+      return true;
+    if (launch_t010(vs, bt->d_jobs, bt->d_items + off_t010 + bt->t010.size(),
+                    (uint32_t)bt->t010b.size(),
+                    bt->d_counters + (kT010Counter + 1) * kCounterStride,
+                    (uint32_t)bt->t010b_stage))
       return true;
   }
   for (int k = 0; k < kSideStreams; ++k) {
