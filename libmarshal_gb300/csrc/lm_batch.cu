@@ -1520,6 +1520,9 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
       // large jobs of units of kStagedMaxUnit bytes and more: cycle
       // following in the planner (2 x payload) is at least as fast
       if (unit >= kStagedMaxUnit && bytes >= kStashPreferBytes) goto planner;
+      // a large job through scratch runs as the planner's own staged form
+      // (its gather and copy back overlap the other jobs on a side stream)
+      if (bytes >= kStashPreferBytes) goto planner;
       // staged: the job fits the arena (in the current wave or a new one)
       if (stageable) {
         if (bt->nwaves == 0 || wave_used + foot > arena_cap) {
