@@ -43,6 +43,10 @@ constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
 // form (the stash moves 3 x payload, the staged form 4 x)
 constexpr uint64_t kStashPreferBytes = 64ull << 20;
 constexpr int kSideStreams = 6;      // streams of the large jobs and groups
+// jobs at least this large that go through scratch run as the planner's
+// staged form on a side stream (measured on the serving trace and the
+// 4096-matrix batch: 4 and 64 MB were both slower)
+constexpr uint64_t kPlannerStagedBytes = 16ull << 20;
 // small jobs of one-element units whose output rows are whole 16-byte
 // vectors (a*e a multiple of 16, aligned buffer) with tiles of at most
 // this size go to the batched 16-byte tile kernel, in items of about
@@ -1522,7 +1526,7 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
       if (unit >= kStagedMaxUnit && bytes >= kStashPreferBytes) goto planner;
       // a large job through scratch runs as the planner's own staged form
       // (its gather and copy back overlap the other jobs on a side stream)
-      if (bytes >= kStashPreferBytes) goto planner;
+      if (bytes >= kPlannerStagedBytes) goto planner;
       // staged: the job fits the arena (in the current wave or a new one)
       if (stageable) {
         if (bt->nwaves == 0 || wave_used + foot > arena_cap) {
