@@ -74,10 +74,12 @@ int prepare_launch(const void *kern, LaunchCache &c, size_t smem, int threads,
 
 // ---- planner thresholds (the per-op planner and the batch executor) ------
 // Measured on GB300 with 256 MB matrices: the staged form (4 x payload
-// through scratch) beats cycle following on units below 512 bytes; the
+// through scratch) beats cycle following on units below 512 bytes, ties it
+// from 512 to 1023 bytes on one tile and beats it on many small tiles
+// (0100(18, 72, 100, 100) of 800-byte units: 2.49 vs 1.60 TB/s); the
 // stash (3 x payload) needs about 48 rows per SM to keep its wavefront fed,
 // and below that the staged form is faster.
-constexpr uint64_t kStagedMaxUnit = 512;
+constexpr uint64_t kStagedMaxUnit = 1024;
 constexpr uint64_t kStashRowsPerSm = 48;
 
 // ---- 010 tiles with 16-byte accesses (lm_tile010.cu) ----------------------
