@@ -12,7 +12,9 @@
 //    AoS -> ASTA conversions): the chunk lands unchanged in shared memory;
 //    a thread builds one output vector from 16/e consecutive rows of one
 //    column -- lanes on consecutive columns, so the shared reads are free
-//    of bank conflicts -- and stores it;
+//    of bank conflicts -- and stores it.  When a*e is only a multiple of 8
+//    or 4, the output vectors are 8 or 4 bytes and the chunk (no longer
+//    16-byte aligned) is loaded as its 16-byte aligned superset;
 //  * form B, B*e a multiple of 16 (every input row is whole vectors; the
 //    ASTA -> AoS conversions): rows land at a pitch of an odd number of
 //    16-byte words; a thread reads one 16-byte piece of a row -- lanes on
@@ -33,7 +35,7 @@ namespace lm {
 
 constexpr int kT010Threads = 256;
 constexpr uint32_t kT010Chunk = 16 * 1024;     // target input bytes per chunk
-constexpr uint32_t kT010MaxTile = 112 * 1024;  // larger tiles: k_bs0100
+constexpr uint32_t kT010MaxTile = 112 * 1024;  // larger: the cluster form
 
 struct T010Args {
   char *base;        // 16-byte aligned
