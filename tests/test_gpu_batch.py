@@ -195,3 +195,30 @@ def test_batch_cluster_off_matches(cuda):
         outs.append([b.cpu().numpy() for b in bufs])
     for x, y in zip(*outs):
         assert np.array_equal(x, y)
+
+
+def test_batch_vector_tile_items(cuda):
+    """AoS->ASTA jobs on 16-byte aligned buffers whose output rows are whole
+    16-byte vectors: tiles up to 16 KB (several per item) and of 16-112 KB
+    (one per item) run through the batched 16-byte tile kernel, beside jobs
+    it does not take (ASTA->AoS, odd tiles), with and without graph
+    replay; every result against the oracle."""
+    from libmarshal_gb300 import lm
+    specs = []
+    for k, (h, w, t, e) in enumerate([
+            (64 * 30, 11, 64, 1), (32 * 50, 7, 32, 4), (16 * 40, 200, 16, 8),
+            (64 * 9, 700, 64, 1), (32 * 8, 1000, 32, 2), (16 * 6, 900, 16, 8),
+            (32 * 100, 3, 32, 2), (64 * 3, 1700, 64, 1)]):
+        specs.append((lm.OP_AOS_ASTA, (h, w, t), e))
+        specs.append((lm.OP_ASTA_AOS, (h, w, t), e))
+    specs.append((lm.OP_010, (40, 12, 5), 1))
+    lm.prof_collect()
+    lm.prof_enable(True)
+    try:
+        st = run_and_check(cuda, specs, graph=False, reps=1)
+        run_and_check(cuda, specs, graph=True, reps=3)
+    finally:
+        lm.prof_enable(False)
+    ran = lm.prof_collect()
+    assert "batch_tile010" in ran, ran
+    assert st["small_jobs"] > 0
