@@ -209,7 +209,7 @@ __device__ void batch_item(const BJob &j, const BItem &it, unsigned char *smem) 
 }
 
 __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_bs(BatchArgs g) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint32_t s_item;
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1u);

@@ -56,7 +56,7 @@ constexpr uint32_t kBandMaxRows = 1024;  // rows of a tile in cluster form
 template <int E>
 __global__ void __launch_bounds__(kBsThreads) k_bs0100(BsArgs g) {
   using T = typename Elem<E>::T;
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   const uint32_t C = 1, rank = 0;
   const uint64_t cid = blockIdx.x, ncl = gridDim.x;
 

@@ -43,6 +43,14 @@ cudaEvent_t take_event() {
 ProfScope::ProfScope(cudaStream_t s, const char *name) : s_(s), name_(name) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
   if (!g_enabled.load(std::memory_order_relaxed)) return;
+  // launches recorded into a graph are not timed (their events would
+  // belong to the graph, not to a run of it)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return;
+  }
   std::lock_guard<std::mutex> lock(g_mu);
   a_ = take_event();
   b_ = take_event();
@@ -76,9 +84,12 @@ int lm_prof_collect(lm_prof_entry *out, int cap) {
   }
   std::vector<lm_prof_entry> acc;
   for (const Rec &r : recs) {
-    cudaEventSynchronize(r.b);
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, r.a, r.b);
+    if (cudaEventSynchronize(r.b) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) {
+      cudaGetLastError();  // leave no error behind for the next call
+      ms = 0.f;
+    }
     size_t i = 0;
     for (; i < acc.size(); ++i)
       if (strncmp(acc[i].name, r.name, sizeof(acc[i].name) - 1) == 0) break;
