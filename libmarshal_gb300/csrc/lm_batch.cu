@@ -36,7 +36,7 @@ constexpr int kMaxWaves = 32;        // staged waves per batch
 constexpr int kCounterStride = 32;   // counters 128 bytes apart
 // small, big, one per cluster size, two per staged wave
 constexpr size_t kCounterBytes =
-    (size_t)(4 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
+    (size_t)(5 + kBandGroups + 2 * kMaxWaves) * kCounterStride * 4;
 constexpr int kT010Counter = 2 + kBandGroups + 2 * kMaxWaves;
 constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
 // jobs at least this large that the stash plan applies to skip the staged
@@ -75,6 +75,10 @@ struct BJob {
   uint32_t ng8;
   FastDiv div_ng8;
   FastDiv div_na;  // a*e/16: 16-byte vectors per output row (tile kernel)
+  // tile kernel, form B (input rows of whole 16-byte vectors): staged row
+  // pitch, 16-byte pieces per row, rows of a full item and its tiles
+  uint32_t tpitch, kt;
+  FastDiv div_nc, div_rows;
 };
 
 struct BItem {
@@ -410,6 +414,41 @@ __device__ __forceinline__ void t010_item_store(const BJob &j, const BItem &it,
   }
 }
 
+// Form B of the same (input rows of whole 16-byte vectors, the ASTA -> AoS
+// conversions): rows were staged at an odd number of 16-byte words; lanes
+// on consecutive rows read 16-byte pieces and scatter their elements into
+// the item's output image (`img`), which is then stored in 16-byte vectors.
+template <int E>
+__device__ __forceinline__ void t010b_item_store(const BJob &j, const BItem &it,
+                                                 const unsigned char *cur,
+                                                 unsigned char *img) {
+  using T = typename Elem<E>::T;
+  constexpr uint32_t VE = 16 / E;
+  const uint32_t B = j.row_elems, R = B * E, NC = R / 16;
+  const uint32_t tb_bytes = j.tile_elems * E;
+  const uint32_t rows = it.ntiles * j.a;
+  const FastDiv dr = it.ntiles == j.kt ? j.div_rows : make_fastdiv(rows);
+  const uint32_t ostep = j.a * E;  // output row bytes
+  for (uint32_t x = threadIdx.x; x < rows * NC; x += kBatchThreads) {
+    const uint32_t pc = fdiv(x, dr);
+    const uint32_t gi = x - pc * rows;
+    const uint32_t t = fdiv(gi, j.div_a);
+    const uint32_t i = gi - t * j.a;
+    const uint4 v = *reinterpret_cast<const uint4 *>(cur + gi * j.tpitch + pc * 16);
+    unsigned char *o = img + t * tb_bytes + (pc * VE * j.a + i) * E;
+#pragma unroll
+    for (uint32_t k = 0; k < VE; ++k)
+      *reinterpret_cast<T *>(o + k * ostep) = vec_elem<E>(v, k);
+  }
+  __syncthreads();  // the output image is complete
+  char *dst = j.base + it.tile0 * (uint64_t)tb_bytes;
+  const uint32_t nv = it.ntiles * (tb_bytes / 16);
+  for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads)
+    __stcg(reinterpret_cast<uint4 *>(dst) + v,
+           *reinterpret_cast<const uint4 *>(img + (size_t)v * 16));
+}
+
+template <bool FB>
 __global__ void __launch_bounds__(kBatchThreads) k_batch_t010(BatchArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint32_t s_item[2];
@@ -435,8 +474,14 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_t010(BatchArgs g) {
     const char *src = j.base + it.tile0 * tbytes;
     const uint32_t nv = (uint32_t)(it.ntiles * tbytes / 16);
     unsigned char *buf = smem + (size_t)sl * g.stage_bytes;
-    for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads)
-      cp_async16(buf + (size_t)v * 16, src + (uint64_t)v * 16);
+    for (uint32_t v = threadIdx.x; v < nv; v += kBatchThreads) {
+      uint32_t off = v * 16;
+      if (FB) {  // rows at their padded pitch
+        const uint32_t row = fdiv(v, j.div_nc);
+        off = row * j.tpitch + (v - row * j.div_nc.d) * 16;
+      }
+      cp_async16(buf + off, src + (uint64_t)v * 16);
+    }
     cp_async_commit();
   };
   if (!claim(0)) return;
@@ -454,11 +499,21 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_t010(BatchArgs g) {
     __syncthreads();  // item n staged by every thread's copies
     const BJob &j = s_jobs[st];
     const unsigned char *cur = smem + (size_t)st * g.stage_bytes;
-    switch (j.e) {
-      case 1: t010_item_store<1>(j, s_it[st], cur); break;
-      case 2: t010_item_store<2>(j, s_it[st], cur); break;
-      case 4: t010_item_store<4>(j, s_it[st], cur); break;
-      default: t010_item_store<8>(j, s_it[st], cur); break;
+    if (FB) {
+      unsigned char *img = smem + 2 * (size_t)g.stage_bytes;
+      switch (j.e) {
+        case 1: t010b_item_store<1>(j, s_it[st], cur, img); break;
+        case 2: t010b_item_store<2>(j, s_it[st], cur, img); break;
+        case 4: t010b_item_store<4>(j, s_it[st], cur, img); break;
+        default: t010b_item_store<8>(j, s_it[st], cur, img); break;
+      }
+    } else {
+      switch (j.e) {
+        case 1: t010_item_store<1>(j, s_it[st], cur); break;
+        case 2: t010_item_store<2>(j, s_it[st], cur); break;
+        case 4: t010_item_store<4>(j, s_it[st], cur); break;
+        default: t010_item_store<8>(j, s_it[st], cur); break;
+      }
     }
     __syncthreads();  // stage st and slot st free
     if (!more) break;
@@ -1136,6 +1191,7 @@ struct lm_batch_st {
   std::vector<lm::BItem> small, big;
   std::vector<lm::BItem> t010;  // items of the batched 16-byte tile kernel
   std::vector<lm::BItem> t010b;  // the same, one larger tile per item
+  std::vector<lm::BItem> t010f;  // its form B (whole-vector input rows)
   size_t t010b_stage = 0;       // bytes of the largest such tile
   std::vector<lm::BItem> band[lm::kBandGroups];  // cluster of 2 << g CTAs
   size_t band_smem[lm::kBandGroups] = {};
@@ -1283,6 +1339,13 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.ng8 = (uint32_t)((nz.a + 7) / 8);
   j.div_ng8 = make_fastdiv(j.ng8);
   j.div_na = make_fastdiv((uint32_t)std::max<uint64_t>(1, nz.a * nz.e / 16));
+  {
+    const uint32_t R = (uint32_t)(nz.B * nz.b * nz.e);
+    j.tpitch = (R / 16) & 1 ? R : R + 16;  // an odd number of 16-byte words
+    j.div_nc = make_fastdiv(std::max<uint32_t>(1, R / 16));
+    j.kt = 1;
+    j.div_rows = make_fastdiv((uint32_t)std::max<uint64_t>(1, nz.a));
+  }
   j.scratch = nullptr;
   j.S = j.Sj = j.nJ = j.nIJ = j.nv16 = 0;
   j.bytes = 0;
@@ -1368,6 +1431,7 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
   bt->t010.clear();
   bt->t010b.clear();
   bt->t010b_stage = 0;
+  bt->t010f.clear();
   bt->big.clear();
   for (int gi = 0; gi < kBandGroups; ++gi) {
     bt->band[gi].clear();
@@ -1581,23 +1645,30 @@ static bool plan_batch(lm_batch_t bt, const lm_job *jobs, int n,
     const uint64_t tile_bytes = tile_elems * (uint64_t)e;
     // whole-vector output rows on an aligned buffer: the batched 16-byte
     // tile kernel (items of about kT010BatchBytes), else the general one
-    const bool vec = nz.b == 1 && ((uintptr_t)jb.buf & 15) == 0 &&
-                     (nz.a * (uint64_t)e) % 16 == 0 &&
-                     tile_bytes <= kT010BatchBytes && !getenv("LM_NO_TILE010");
-    uint64_t k_t = vec ? std::max<uint64_t>(1, kT010BatchBytes / tile_bytes)
+    const bool vec_ok = nz.b == 1 && ((uintptr_t)jb.buf & 15) == 0 &&
+                        tile_bytes <= kT010BatchBytes && !getenv("LM_NO_TILE010");
+    const bool vec = vec_ok && (nz.a * (uint64_t)e) % 16 == 0;
+    const bool vecb = vec_ok && !vec && (nz.B * (uint64_t)e) % 16 == 0;
+    uint64_t k_t = (vec || vecb)
+                       ? std::max<uint64_t>(1, kT010BatchBytes / tile_bytes)
                        : std::max<uint64_t>(1, kSmallItem / tile_smem);
     while (k_t > 1 && k_t * tile_elems >= 0xffffffffull) --k_t;
+    if (vecb) {  // rows of a full item for the form-B store
+      bt->jobs[jid].kt = (uint32_t)k_t;
+      bt->jobs[jid].div_rows = make_fastdiv((uint32_t)(k_t * nz.a));
+    }
     for (uint64_t t0 = 0; t0 < nz.T; t0 += k_t) {
       BItem it;
       it.job = jid;
       it.tile0 = t0;
       it.ntiles = (uint32_t)std::min<uint64_t>(k_t, nz.T - t0);
-      (vec ? bt->t010 : bt->small).push_back(it);
+      (vec ? bt->t010 : vecb ? bt->t010f : bt->small).push_back(it);
     }
     bt->stats.small_jobs += 1;
     bt->stats.small_bytes += bytes;
   }
-  bt->stats.small_items = bt->small.size() + bt->t010.size() + bt->t010b.size();
+  bt->stats.small_items = bt->small.size() + bt->t010.size() +
+                          bt->t010b.size() + bt->t010f.size();
   bt->stats.big_items = bt->big.size();
   for (int gi = 0; gi < kBandGroups; ++gi)
     bt->stats.band_items += bt->band[gi].size();
@@ -1800,13 +1871,14 @@ static bool launch_small(cudaStream_t s, const BJob *d_jobs,
 
 static bool launch_t010(cudaStream_t s, const BJob *d_jobs,
                         const BItem *d_items, uint32_t nitems,
-                        uint32_t *counter, uint32_t stage) {
+                        uint32_t *counter, uint32_t stage, bool form_b) {
   if (nitems == 0) return false;
-  const size_t smem = 2 * (size_t)stage;
-  static LaunchCache cache;
+  const size_t smem = 2 * (size_t)stage + (form_b ? kT010BatchBytes : 0);
+  static LaunchCache cache_a, cache_b;
+  auto kern = form_b ? k_batch_t010<true> : k_batch_t010<false>;
   cudaError_t err = cudaSuccess;
-  const int occ = prepare_launch((const void *)k_batch_t010, cache, smem,
-                                 kBatchThreads, &err);
+  const int occ = prepare_launch((const void *)kern, form_b ? cache_b : cache_a,
+                                 smem, kBatchThreads, &err);
   if (err != cudaSuccess || occ < 1) return set_error("batch: tile kernel setup");
   const DeviceInfo &di = device_info();
   const uint32_t grid =
@@ -1819,7 +1891,7 @@ static bool launch_t010(cudaStream_t s, const BJob *d_jobs,
   g.status = nullptr;
   g.stage_bytes = stage;
   ProfScope ps(s, "batch_tile010");
-  k_batch_t010<<<grid, kBatchThreads, smem, s>>>(g);
+  kern<<<grid, kBatchThreads, smem, s>>>(g);
   if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
   return false;
 }
@@ -1853,7 +1925,7 @@ static bool launch_items(cudaStream_t s, const BJob *d_jobs,
 // Records the work of the planned batch on stream s.
 static size_t item_count(lm_batch_t bt) {
   size_t n = bt->small.size() + bt->big.size() + bt->t010.size() +
-             bt->t010b.size();
+             bt->t010b.size() + bt->t010f.size();
   for (int gi = 0; gi < kBandGroups; ++gi) n += bt->band[gi].size();
   for (int w = 0; w < bt->nwaves; ++w)
     n += bt->wgather[w].size() + bt->wcopy[w].size();
@@ -1960,6 +2032,7 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
     }
     put(bt->t010);
     put(bt->t010b);
+    put(bt->t010f);
   }
   if (nj && cudaMemcpyAsync(bt->d_jobs, h, nj * sizeof(BJob),
                             cudaMemcpyHostToDevice, s) != cudaSuccess)
@@ -1997,7 +2070,7 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   int nq = 0;
   cudaStream_t q[1 + kBandGroups + 2];
   int ngroups = (bt->nwaves > 0) + (!bt->small.empty() || !bt->big.empty()) +
-                (!bt->t010.empty() || !bt->t010b.empty());
+                (!bt->t010.empty() || !bt->t010b.empty() || !bt->t010f.empty());
   for (int gi = 0; gi < kBandGroups; ++gi) ngroups += !bt->band[gi].empty();
   if (ngroups > 1) {
     if (ensure_side(bt)) return true;
@@ -2051,17 +2124,24 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
         return true;
     }
   }
-  if (!bt->t010.empty() || !bt->t010b.empty()) {
+  if (!bt->t010.empty() || !bt->t010b.empty() || !bt->t010f.empty()) {
     const cudaStream_t vs = next_stream();
-    if (launch_t010(vs, bt->d_jobs, bt->d_items + off_t010,
-                    (uint32_t)bt->t010.size(),
+    size_t o = off_t010;
+    if (launch_t010(vs, bt->d_jobs, bt->d_items + o, (uint32_t)bt->t010.size(),
                     bt->d_counters + kT010Counter * kCounterStride,
-                    kT010BatchBytes))
+                    kT010BatchBytes, false))
       return true;
-    if (launch_t010(vs, bt->d_jobs, bt->d_items + off_t010 + bt->t010.size(),
-                    (uint32_t)bt->t010b.size(),
+    o += bt->t010.size();
+    if (launch_t010(vs, bt->d_jobs, bt->d_items + o, (uint32_t)bt->t010b.size(),
                     bt->d_counters + (kT010Counter + 1) * kCounterStride,
-                    (uint32_t)bt->t010b_stage))
+                    (uint32_t)bt->t010b_stage, false))
+      return true;
+    o += bt->t010b.size();
+    // form B: rows padded by at most 16 bytes each (at most twice the
+    // item's bytes per stage) and an output image of the item's size
+    if (launch_t010(vs, bt->d_jobs, bt->d_items + o, (uint32_t)bt->t010f.size(),
+                    bt->d_counters + (kT010Counter + 2) * kCounterStride,
+                    2 * kT010BatchBytes, true))
       return true;
   }
   for (int k = 0; k < kSideStreams; ++k) {
