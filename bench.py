@@ -223,7 +223,7 @@ def run_reference(args, ws, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(el / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (splitmix64 random bits)",
+        "dtype": "f32", "data": "synthetic (seeded random bits)",
         "config": CONFIG, "impl": "reference",
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT,
                          "cores": threads, "kind": "port", "sample": sample},
@@ -310,11 +310,20 @@ def run_ours(args, ws, rank, local):
     prof = lm.prof_collect()
     ms_prof = ep0.elapsed_time(ep1)
 
-    # restore the input (even number of steps) and verify on the device
+    # restore the input (even number of steps) and verify on the device:
+    # the round trip, and one forward conversion against the closed-form
+    # index map (element (i, j) of the [A][B] input lands at j*A + i), i.e.
+    # torch's out-of-place transpose of the kept copy
     if count[0] & 1:
         step()
     torch.cuda.synchronize()
-    verified = bool(torch.equal(buf, orig))
+    round_trip = bool(torch.equal(buf, orig))
+    step()  # (A0, B0) -> [B0][A0]
+    torch.cuda.synchronize()
+    forward = bool(torch.equal(buf.view(B0, A0), orig.view(A0, B0).t()))
+    step()  # and back
+    torch.cuda.synchronize()
+    verified = round_trip and forward and bool(torch.equal(buf, orig))
     del orig
 
     value = aggregate_rate(ws, 2.0 * PAYLOAD, args.steps, ms)
@@ -409,8 +418,10 @@ def run_ours(args, ws, rank, local):
             "ms_per_step": round(ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded random bits)",
-            "config": dict(CONFIG, parallelism="replicas" if ws > 1 else
-                           "single GPU", verified_round_trip=verified),
+            "config": CONFIG,
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "verified": {"all": verified, "round_trip": round_trip,
+                         "forward_vs_closed_form_map": forward},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk, "gpu_launches": int(launches),
         }
@@ -444,6 +455,7 @@ def batch_specs(n=4096, seed=1, lo=16, hi=4096):
 
 
 def run_batch_workload(args, ws, rank, local):
+    import numpy as np
     import torch
     import __graft_entry__
     __graft_entry__.build()
@@ -498,7 +510,8 @@ def run_batch_workload(args, ws, rank, local):
     ms_plain, l_plain = (float("nan"), 0) if args.skip_plain else \
         timed(plain_step, k, w)
     ms_batch, l_batch = timed(lambda: bt.run(jobs, stream=stream), k, w)
-    ms_graph, _ = timed(lambda: bt.run(jobs, stream=stream, graph=True), k, w)
+    ms_graph, l_graph = timed(lambda: bt.run(jobs, stream=stream, graph=True),
+                              k, w)
     lm.prof_collect()
     lm.prof_enable(True)
     bt.run(jobs, stream=stream)
@@ -507,35 +520,117 @@ def run_batch_workload(args, ws, rank, local):
     kern = {n: {"launches": v[0], "ms": round(v[1], 3)}
             for n, v in lm.prof_collect().items()}
     st = bt.stats()
+
+    # verification (outside every timed region): each job's region gets a
+    # seeded input, one run of each form converts the whole list, and every
+    # job is compared with the oracle
+    verified = None
+    if not args.no_verify:
+        from oracle import check as C
+        vjobs = [(off, C.OP_AOS_ASTA if op == "aos_asta" else C.OP_TRANSPOSE,
+                  d, e) for (op, d, e), off in zip(specs, offs)]
+        arena_u8 = arena.view(torch.uint8)
+        verified = {}
+        forms = [("batched", lambda: bt.run(jobs, stream=stream)),
+                 ("batched_graph",
+                  lambda: bt.run(jobs, stream=stream, graph=True))]
+        if not args.skip_plain:
+            forms.append(("plain_loop", plain_step))
+        for name, fn in forms:
+            host = np.empty(tot, dtype=np.uint8)
+            C.fill_host(host, vjobs, 1 << 20)
+            arena_u8[:tot].copy_(torch.from_numpy(host))
+            del host
+            fn()
+            torch.cuda.synchronize()
+            got = arena_u8[:tot].cpu().numpy()
+            bad = C.check_host(got, vjobs, 1 << 20)
+            del got
+            verified[name] = {"jobs": len(vjobs), "mismatched": len(bad),
+                              "first_bad": bad[:5]}
+        verified["all"] = all(v["mismatched"] == 0 for v in verified.values())
+
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_batch_rate(specs)
     bt.close()
     gbs = lambda ms: 2.0 * payload / (ms / 1e3) / 1e9
     peak, peak_kind = peak_hbm()
+    use_graph = ms_graph <= ms_batch
+    ms_best = ms_graph if use_graph else ms_batch
     line = {
-        "metric": "batched_conversion_GBps", "value": round(gbs(ms_graph), 2),
+        "metric": "batched_conversion_GBps", "value": round(gbs(ms_best), 2),
         "unit": "GB/s", "n_gpus": ws, "steps": k, "warmup": w,
-        "ms_per_step": round(ms_graph, 3), "higher_is_better": True,
+        "ms_per_step": round(ms_best, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "mixed u8/u16/u32/u64",
         "data": "synthetic (seeded random bits)",
         "config": {"workload": "batch_4096_mixed_aos_asta_transpose",
                    "matrices": len(specs), "payload_bytes": payload,
                    "dims": "log-uniform [16, 4096] per side, seed 1",
-                   "l2": "payload %.1f GB >> L2" % (payload / 1e9)},
+                   "l2": "payload %.1f GB >> L2" % (payload / 1e9),
+                   "form_reported": "graph replay" if use_graph else
+                                    "batched without graph (faster here)"},
+        "verified": verified,
         "plain_loop": {"value": round(gbs(ms_plain), 2), "ms_per_step":
                        round(ms_plain, 3), "kernel_launches": int(l_plain)},
         "batched_no_graph": {"value": round(gbs(ms_batch), 2), "ms_per_step":
                              round(ms_batch, 3), "kernel_launches": int(l_batch)},
         "batched_graph": {"value": round(gbs(ms_graph), 2),
-                          "ms_per_step": round(ms_graph, 3)},
-        "speedup_vs_plain": round(ms_plain / ms_graph, 2),
-        "frac_of_peak": round(gbs(ms_graph) / peak, 4), "peak": peak,
-        "peak_kind": peak_kind, "batch_stats": st,
+                          "ms_per_step": round(ms_graph, 3),
+                          "kernel_launches": int(l_graph)},
+        "speedup_vs_plain": round(ms_plain / ms_best, 2),
+        "roofline": {"bound": "hbm", "achieved": round(gbs(ms_best), 1),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(gbs(ms_best) / peak, 4), "traffic": None,
+                     "kernel": "whole batched step (concurrent kernels on "
+                               "side streams)", "peak_kind": peak_kind},
+        "cpu_baseline": cpu, "batch_stats": st,
         "tuned_shape_classes": int(L.lm_tune_entries()),
         "kernels_one_batched_step": kern,
+        "gpu_launches": int(l_graph if use_graph else l_batch),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    return 0
+    ok = verified is None or verified["all"]
+    return 0 if ok else 3
 
+
+def cpu_batch_rate(specs, seconds=1.5):
+    """GB/s of the reference's out-of-place CPU layout loops (cpu_aos_asta /
+    the full-transpose golden, restated in the oracle) over the same job
+    list, jobs in parallel on every host thread, on a bounded prefix of the
+    list (whole jobs until `seconds` of work)."""
+    import numpy as np
+    from oracle import check as C
+    vj = [(C.OP_AOS_ASTA if op == "aos_asta" else C.OP_TRANSPOSE, d, e)
+          for (op, d, e) in specs]
+    srcs = []
+    t_gen = 0
+    for k, (op, d, e) in enumerate(vj):
+        srcs.append(C.job_input(C.n_elems(op, d), e, k))
+        t_gen += srcs[-1].nbytes
+        if t_gen > (2 << 30):
+            break
+    n = len(srcs)
+    with C.pool() as ex:
+        list(ex.map(lambda k: C.expected(vj[k][0], vj[k][1], srcs[k]),
+                    range(min(n, 64))))  # warm
+        t0 = time.perf_counter()
+        done_b, done_j = 0, 0
+        while True:
+            list(ex.map(lambda k: C.expected(vj[k][0], vj[k][1], srcs[k]),
+                        range(n)))
+            done_b += sum(s.nbytes for s in srcs)
+            done_j += n
+            el = time.perf_counter() - t0
+            if el >= seconds:
+                break
+    return {"value": round(2.0 * done_b / el / 1e9, 3), "unit": "GB/s",
+            "cores": C.threads(), "kind": "port",
+            "sample": "the list's first %d jobs (%.2f GB), converted %d times "
+                      "in %.2f s, jobs spread over %d threads"
+                      % (n, sum(s.nbytes for s in srcs) / 1e9, done_j // n, el,
+                         C.threads())}
 
 
 # ---- every measured configuration (plain per-op calls, CPU 1 and N threads) ---
@@ -806,6 +901,62 @@ def run_serve_workload(args, ws, rank, local):
                 row[mode]["peak_inflight_GB"] = round(
                     st["peak_inflight_bytes"] / 1e9, 2)
         results.append(row)
+        last = (reqs, arrival, after, trace, spans)
+
+    # verification at the top rate (outside the timed replays): every
+    # request's region gets a seeded input, the trace is replayed at its
+    # arrival times (served: in the mix; plain: alone, one request per
+    # call), and every result is compared with the oracle
+    verified = None
+    if not args.no_verify and results:
+        from oracle import check as C
+        reqs, arrival, after, trace, spans = last
+        arena_u8 = arena.view(torch.uint8)
+        # a request whose bytes a later request reuses (ring wrap) cannot be
+        # checked at the end; with the default ring nothing wraps
+        reused = set()
+        for k in range(len(spans)):
+            for j in range(k + 1, len(spans)):
+                if spans[j][0] < spans[k][1] and spans[k][0] < spans[j][1]:
+                    reused.add(k)
+                    break
+        vjobs = [(spans[k][0], code[op], dims, e)
+                 for k, (_, op, dims, e) in enumerate(trace)]
+        check_ids = [k for k in range(len(vjobs)) if k not in reused]
+        verified = {"rate_per_s": results[-1]["rate_per_s"],
+                    "requests_checked": len(check_ids),
+                    "requests_not_checkable": len(reused)}
+
+        def fill(k):
+            off, op, dims, e = vjobs[k]
+            n = C.n_elems(op, dims) * e
+            src = C.job_input(C.n_elems(op, dims), e, (2 << 20) + k)
+            arena_u8[off:off + n].copy_(torch.from_numpy(src.view(np.uint8)))
+
+        def check(k):
+            off, op, dims, e = vjobs[k]
+            n = C.n_elems(op, dims)
+            got = arena_u8[off:off + n * e].cpu().numpy().view(C.O.DTYPES[e])
+            want = C.expected(op, dims, C.job_input(n, e, (2 << 20) + k))
+            return None if np.array_equal(got, want) else k
+
+        for mode in ("served", "plain"):
+            with C.pool() as ex:
+                list(ex.map(fill, range(len(vjobs))))
+            torch.cuda.synchronize()
+            srv = None if mode == "plain" else lm.Server(budget)
+            res = lm.serve_replay(srv, reqs, arrival, after,
+                                  plain=(mode == "plain"))
+            if srv is not None:
+                srv.close()
+            torch.cuda.synchronize()
+            with C.pool() as ex:
+                bad = [k for k in ex.map(check, check_ids) if k is not None]
+            verified[mode] = {"failed_status": sum(1 for r in res if r[0]),
+                              "mismatched": len(bad), "first_bad": bad[:5]}
+        verified["all"] = all(verified[m]["mismatched"] == 0 and
+                              verified[m]["failed_status"] == 0
+                              for m in ("served", "plain"))
     peak, peak_kind = peak_hbm()
     top = results[-1]
     line = {
@@ -822,11 +973,56 @@ def run_serve_workload(args, ws, rank, local):
                    "warmup": "the trace's first 200 requests, untimed, "
                              "before each timed replay"},
         "p50_ms": top["served"]["p50_ms"], "p99_ms": top["served"]["p99_ms"],
+        "plain": {"value": top["plain"]["GBps"],
+                  "p50_ms": top["plain"]["p50_ms"],
+                  "p99_ms": top["plain"]["p99_ms"]},
+        "served_over_plain": round(top["served"]["GBps"] /
+                                   top["plain"]["GBps"], 3),
+        "verified": verified,
+        "roofline": {"bound": "hbm", "achieved": top["served"]["GBps"],
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(top["served"]["GBps"] / peak, 4),
+                     "traffic": None,
+                     "kernel": "whole served trace (2 x payload / makespan)",
+                     "peak_kind": peak_kind},
+        "cpu_baseline": None if args.no_cpu else cpu_serve_rate(last[3]),
         "peak": peak, "peak_kind": peak_kind, "rates": results,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    return 0
+    return 0 if verified is None or verified["all"] else 3
+
+
+def cpu_serve_rate(trace, seconds=1.5):
+    """GB/s of the reference's CPU layout loops (restated in the oracle) on
+    the trace's requests in arrival order, requests spread over every host
+    thread, until `seconds` of work (a bounded prefix of the trace)."""
+    from oracle import check as C
+    code = {"aos_asta": C.OP_AOS_ASTA, "asta_aos": C.OP_ASTA_AOS,
+            "soa_asta": C.OP_SOA_ASTA, "asta_soa": C.OP_ASTA_SOA,
+            "transpose": C.OP_TRANSPOSE}
+    jobs, tot = [], 0
+    for k, (_, op, dims, e) in enumerate(trace):
+        n = C.n_elems(code[op], dims)
+        jobs.append((code[op], dims, C.job_input(n, e, k)))
+        tot += n * e
+        if tot > (4 << 30):
+            break
+    t0 = time.perf_counter()
+    done = 0
+    with C.pool() as ex:
+        for i in range(0, len(jobs), C.threads()):
+            part = jobs[i:i + C.threads()]
+            list(ex.map(lambda j: C.expected(j[0], j[1], j[2]), part))
+            done += sum(j[2].nbytes for j in part)
+            if time.perf_counter() - t0 >= seconds:
+                break
+    el = time.perf_counter() - t0
+    return {"value": round(2.0 * done / el / 1e9, 3), "unit": "GB/s",
+            "cores": C.threads(), "kind": "port",
+            "sample": "the trace's first requests in arrival order, %.2f GB "
+                      "converted in %.2f s over %d threads"
+                      % (done / 1e9, el, C.threads())}
 
 def main():
     ap = argparse.ArgumentParser()
@@ -840,6 +1036,8 @@ def main():
                     choices=["headline", "batch", "serve", "configs"])
     ap.add_argument("--batch-n", type=int, default=4096,
                     help="matrices in the batched workload")
+    ap.add_argument("--no-verify", action="store_true",
+                    help="batch/serve workloads: skip the oracle check")
     ap.add_argument("--skip-plain", action="store_true",
                     help="batched workload: skip the per-request loop")
     ap.add_argument("--serve-n", type=int, default=2000,

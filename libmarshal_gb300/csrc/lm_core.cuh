@@ -332,6 +332,22 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
       : "memory");
 }
 
+// L2 eviction-priority policy for st_hint16: lines written under
+// evict_last are chosen last when the L2 needs room.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// 16-byte store with an L2 eviction-priority policy.
+__device__ __forceinline__ void st_hint16(void *p, const uint4 &v,
+                                          uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::
+                   "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(policy)
+               : "memory");
+}
+
 // Cluster barrier halves.  A relaxed arrive orders no memory accesses (use it
 // where the barrier only has to order execution); the default arrive has
 // release semantics and the wait acquire semantics, at cluster scope.

@@ -62,8 +62,7 @@ struct StashArgs {
   uint64_t timeout_ns;
   uint32_t margin;       // stash margin k (steps of slack between CTAs)
   uint32_t tma;          // 1: gather rows with bulk copies, 0: cp.async
-  uint64_t *trace;       // debug: per (chunk, step) timestamps, or null
-  uint32_t trace_ctas;
+  uint32_t jcut;         // K1 saves the wave's first jcut steps' strips last
   // first stashed group of a row (stash_first_group) without a division:
   // i*B and g*(A-1) are < 2^32
   uint64_t gAk;          // g*A*margin
@@ -173,10 +172,43 @@ __global__ void __launch_bounds__(1024) k_stash_offsets(StashArgs sa) {
 
 // K1: copy every row's stash suffix: one warp per row at a time, 16-byte
 // vectors between the (equally misaligned) buffer and stash addresses, the
-// ragged head and tail bytes one by one.
+// ragged head and tail bytes one by one.  In two passes: first the part of
+// each suffix that the wave reads after its first jcut steps, with
+// evict-first stores, then the part those steps read (their strips, about
+// 30 MB for the fp32 16384 x 12289 transposition), with evict-last stores,
+// so that most of it is still in L2 when the wave starts (0.8 % faster).
 constexpr int kSaveThreads = 256;
+constexpr uint32_t kStashEarlySteps = 20;
+
+// Copies n bytes from src to dst (equal addresses modulo 16) with one warp;
+// last: evict-last stores under `policy`, else evict-first stores.
+__device__ __forceinline__ void save_bytes(const char *src, char *dst,
+                                           uint64_t n, uint32_t lane,
+                                           bool last, uint64_t policy) {
+  const uint64_t head = min64((16 - ((uintptr_t)src & 15)) & 15, n);
+  const uint64_t nvec = (n - head) / 16;
+  const uint64_t tail0 = head + nvec * 16;
+  if (lane < head) dst[lane] = src[lane];
+  if (lane < n - tail0) dst[tail0 + lane] = src[tail0 + lane];
+  const uint4 *vs = reinterpret_cast<const uint4 *>(src + head);
+  uint4 *vd = reinterpret_cast<uint4 *>(dst + head);
+  for (uint64_t v = lane; v < nvec; v += 32 * 4) {
+    uint4 x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (v + 32 * u < nvec) x[u] = __ldcs(vs + v + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (v + 32 * u >= nvec) continue;
+      if (last) st_hint16(vd + v + 32 * u, x[u], policy);
+      else __stcs(vd + v + 32 * u, x[u]);
+    }
+  }
+}
 
 __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
+  // the wave may be scheduled onto SMs as this grid's blocks drain
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const uint32_t lane = threadIdx.x & 31;
   // the wave's progress counters start at zero (K2 runs after K1)
   for (uint32_t x = blockIdx.x * kSaveThreads + threadIdx.x;
@@ -185,27 +217,21 @@ __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
   const uint64_t gw = ((uint64_t)blockIdx.x * kSaveThreads + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * kSaveThreads) >> 5;
   const uint64_t U = (uint64_t)g.b * g.e;
-  for (uint64_t i = gw; i < g.A; i += nw) {
-    const uint64_t Ji = first_group(i, g);
-    if (Ji >= g.G) continue;
-    const char *src = g.base + (i * g.B + Ji * g.g) * U;
-    char *dst = g.stash + g.roff[i];
-    const uint64_t n = (g.B - Ji * g.g) * U;
-    const uint64_t head = min64((16 - ((uintptr_t)src & 15)) & 15, n);
-    const uint64_t nvec = (n - head) / 16;
-    const uint64_t tail0 = head + nvec * 16;
-    if (lane < head) dst[lane] = src[lane];
-    if (lane < n - tail0) dst[tail0 + lane] = src[tail0 + lane];
-    const uint4 *vs = reinterpret_cast<const uint4 *>(src + head);
-    uint4 *vd = reinterpret_cast<uint4 *>(dst + head);
-    for (uint64_t v = lane; v < nvec; v += 32 * 4) {
-      uint4 x[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (v + 32 * u < nvec) x[u] = __ldcs(vs + v + 32 * u);
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (v + 32 * u < nvec) __stcg(vd + v + 32 * u, x[u]);
+  const uint64_t pol_last = l2_policy_evict_last();
+  for (int pass = 0; pass < 2; ++pass) {
+    for (uint64_t i = gw; i < g.A; i += nw) {
+      const uint64_t Ji = first_group(i, g);
+      if (Ji >= g.G) continue;
+      const char *src = g.base + (i * g.B + Ji * g.g) * U;
+      char *dst = g.stash + g.roff[i];
+      const uint64_t n = (g.B - Ji * g.g) * U;
+      // strips J_i .. jcut-1 of the row: its first (jcut - J_i) strips
+      const uint64_t early =
+          Ji < g.jcut ? min64(n, (g.jcut - Ji) * (uint64_t)g.g * U) : 0;
+      if (pass == 0)
+        save_bytes(src + early, dst + early, n - early, lane, false, pol_last);
+      else
+        save_bytes(src, dst, early, lane, true, pol_last);
     }
   }
 }
@@ -233,9 +259,6 @@ constexpr int kMaxRowBlocks = 4;  // rows per chunk <= 128
 constexpr uint32_t kStashMargin = 2;
 constexpr uint32_t kMaxChunks = 1024;  // CTAs of the wave (co-resident)
 constexpr uint32_t kProgStride = 32;   // one 128-byte line per progress word
-// LM_STASH_TRACE slots per (chunk, step): 0 gather issued, 1 published,
-// 2 stage ready (deps and ring), 3 written, 4 deps satisfied, 5 check begun
-constexpr int kTraceSlots = 8;
 
 template <int E>
 __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
@@ -274,6 +297,10 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     s_pstop = 0;
   }
   for (uint32_t c = threadIdx.x; c < kMaxChunks; c += blockDim.x) seen[c] = 0;
+  // launched as a programmatic dependent of K1: everything above ran while
+  // K1's last blocks were finishing; K1's writes (stash, cleared progress
+  // counters) are visible after this wait (a no-op without the attribute)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   __syncthreads();
 
   // bounded wait; false on timeout or when another role has failed
@@ -346,8 +373,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
             bytes += __shfl_xor_sync(kFull, bytes, o);
           fence_proxy_async_smem();
           __syncwarp();
-          if (g.trace && ch < g.trace_ctas && lane == 0)
-            g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 0] = global_timer_ns();
           if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
           __syncwarp();
 #pragma unroll
@@ -376,8 +401,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
             cp_async16(sb + (size_t)t * g.pitch + 16 * c,
                        (const void *)(a0 + 16 * (uintptr_t)c));
         }
-        if (g.trace && ch < g.trace_ctas && pt == 0)
-          g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 0] = global_timer_ns();
         cp_async_mbar_arrive_noinc(&full[s]);
       }
     }
@@ -402,8 +425,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
       const bool landed = wait_bar(&full[s], (J / kStages) & 1);
       if (!__all_sync(kFull, landed)) break;
       if (lane == 0) st_release_gpu(g.progress + kProgStride * ch, J + 1);
-      if (g.trace && ch < g.trace_ctas && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 1] = global_timer_ns();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
     // never leave another CTA waiting on this one
@@ -433,8 +454,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     bool good = true;
     for (uint32_t J = 0; J < g.G && good; ++J) {
       const uint32_t s = J % kStages;
-      if (g.trace && ch < g.trace_ctas && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 5] = global_timer_ns();
       const uint32_t need = J + 1 > g.margin ? J + 1 - g.margin : 0u;
       if (need > 0) {
         const uint64_t cf = first_c(J), cl = last_c(J);
@@ -462,8 +481,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
         good = __all_sync(kFull, good);
       }
       if (!good) break;
-      if (g.trace && ch < g.trace_ctas && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 4] = global_timer_ns();
       if (J >= kStages) {
         const bool ok = wait_bar(&empty[s], ((J / kStages) - 1) & 1);
         if (!__all_sync(kFull, ok)) {
@@ -471,8 +488,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
           break;
         }
       }
-      if (g.trace && ch < g.trace_ctas && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 2] = global_timer_ns();
       if (lane == 0) mbar_arrive(&ready[s]);
     }
     if (!good && lane == 0) {
@@ -526,8 +541,6 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
         }
       }
       __syncwarp();
-      if (g.trace && ch < g.trace_ctas && wid == 0 && lane == 0)
-        g.trace[((uint64_t)ch * g.G + J) * kTraceSlots + 3] = global_timer_ns();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
   }
@@ -783,53 +796,31 @@ static cudaError_t run_stash(cudaStream_t s, StashArgs g, const StashPlan &p) {
   if (getenv("LM_VERBOSE"))
     fprintf(stderr, "stash: g=%u G=%u W=%u chunks=%u smem=%zu occ=%d stash=%zu\n",
             p.g, p.G, p.W, p.nchunks, p.smem_bytes, occ, p.stash_bytes);
-  // LM_STASH_TRACE=n: record step timestamps of the first n CTAs and print
-  // a summary (debugging aid; allocates and synchronises).
-  const char *tr = getenv("LM_STASH_TRACE");
-  uint64_t *trace = nullptr;
-  if (tr && atoi(tr) > 0) {
-    g.trace_ctas = (uint32_t)std::min(atoi(tr), (int)p.nchunks);
-    const size_t tb = (size_t)g.trace_ctas * g.G * kTraceSlots * 8;
-    if (cudaMalloc(&trace, tb) == cudaSuccess) {
-      cudaMemsetAsync(trace, 0, tb, s);
-      g.trace = trace;
-    }
-  }
   void *args[] = {&g};
   ProfScope ps(s, "stash_wave");
-  // cooperative launch: every CTA is co-resident, so the waits can end
+  // cooperative launch: every CTA is co-resident, so the waits can end.
+  // It is also a programmatic dependent of K1, so its CTAs are set up on
+  // the SMs that K1's draining blocks free instead of after K1 exits.
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(p.nchunks);
+    cfg.blockDim = dim3(kWaveThreads);
+    cfg.dynamicSmemBytes = p.smem_bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 2;
+    err = cudaLaunchKernelExC(&cfg, (const void *)kern, args);
+    if (err == cudaSuccess) return cudaGetLastError();
+    cudaGetLastError();  // not accepted: plain cooperative launch below
+  }
   err = cudaLaunchCooperativeKernel((const void *)kern, dim3(p.nchunks),
                                     dim3(kWaveThreads), args, p.smem_bytes, s);
   if (err != cudaSuccess) return err;
-  if (trace) {
-    cudaStreamSynchronize(s);
-    const size_t n = (size_t)g.trace_ctas * g.G * kTraceSlots;
-    uint64_t *h = (uint64_t *)malloc(n * 8);
-    cudaMemcpy(h, trace, n * 8, cudaMemcpyDeviceToHost);
-    for (uint32_t c = 0; c < g.trace_ctas; ++c) {
-      double land = 0, deps = 0, wr = 0, per = 0, chk = 0, ring = 0, lead = 0;
-      uint64_t *t = h + (size_t)c * g.G * kTraceSlots;
-      auto at = [&](uint32_t J, int k) { return t[J * kTraceSlots + k]; };
-      auto d = [](uint64_t a, uint64_t b) { return (double)(int64_t)(a - b); };
-      for (uint32_t J = 1; J + 1 < g.G; ++J) {
-        land += d(at(J, 1), at(J, 0));
-        deps += d(at(J, 2), at(J, 1));
-        wr += d(at(J, 3), std::max(at(J, 2), at(J, 1)));
-        per += d(at(J + 1, 3), at(J, 3));
-        chk += d(at(J, 4), at(J, 5));
-        ring += d(at(J, 2), at(J, 4));
-        lead += d(at(J, 1), at(J, 5));
-      }
-      const double k = (double)(g.G - 2) * 1000.0;
-      fprintf(stderr, "stash trace cta %u: issue->published %.2f us, published->ready %.2f us, "
-              "ready->written %.2f us, step period %.2f us; checker: begun %.2f us before "
-              "publish, deps %.2f us, ring %.2f us; total %.1f us\n", c, land / k,
-              deps / k, wr / k, per / k, lead / k, chk / k, ring / k,
-              (double)(at(g.G - 1, 3) - at(0, 0)) / 1000.0);
-    }
-    free(h);
-    cudaFree(trace);
-  }
   return cudaGetLastError();
 }
 
@@ -862,8 +853,6 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   g.div_gb = make_fastdiv(g.gb);
   g.div_b = make_fastdiv(b);
   g.timeout_ns = timeout_ns;
-  g.trace = nullptr;
-  g.trace_ctas = 0;
   g.margin = p.margin;
   g.gAk = (uint64_t)p.g * A * p.margin;
   g.div_D = make_fastdiv((uint32_t)((uint64_t)p.g * (A - 1)));
@@ -872,6 +861,8 @@ cudaError_t launch_stash100(cudaStream_t s, void *buf, int e, uint64_t A,
   {
     const char *gm = getenv("LM_STASH_GATHER");
     g.tma = (gm && gm[0] == 'c') ? 0u : 1u;  // "cpasync" selects cp.async
+    const char *jc = getenv("LM_STASH_EARLY");
+    g.jcut = jc ? (uint32_t)atoi(jc) : kStashEarlySteps;
   }
   switch (e) {
     case 1: return run_stash<1>(s, g, p);

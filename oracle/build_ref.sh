@@ -14,7 +14,10 @@
 # (Transposition is built with a NULL context, plan.hpp:27-30 then uses its
 # defaults), so only the reference's integer arithmetic is exercised.
 #
-# Usage: sh oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: sh oracle/build_ref.sh [reference-root]
+# The root is the argument, else $LM_REFERENCE, else the checkout's place in
+# the build container (/root/reference); where none exists the recipe exits
+# with status 2 and builds nothing.
 set -e
 REF=${1:-${LM_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)

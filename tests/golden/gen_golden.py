@@ -1,8 +1,8 @@
 """Generate tests/golden/golden.json from the reference's OWN CPU code.
 
-Run in a container that has the reference checkout (default /root/reference):
+Run in a container that has the reference checkout, naming its root:
 
-    python tests/golden/gen_golden.py [reference-root]
+    python tests/golden/gen_golden.py <reference-root>   (or LM_REFERENCE=...)
 
 It builds oracle/_ref/libref_cpu.so with oracle/build_ref.sh (the reference's
 cpu_aos_asta / cpu_soa_asta from test/cl_unittest.cc:138-166, the templated
@@ -118,8 +118,9 @@ def full_cases():
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(
-        "LM_REFERENCE", "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LM_REFERENCE")
+    if not ref:
+        sys.exit("usage: gen_golden.py <reference-root> (or set LM_REFERENCE)")
     subprocess.check_call(["sh", os.path.join(ROOT, "oracle", "build_ref.sh"),
                            ref])
     R = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_cpu.so"))

@@ -222,3 +222,47 @@ def test_batch_vector_tile_items(cuda):
     ran = lm.prof_collect()
     assert "batch_tile010" in ran, ran
     assert st["small_jobs"] > 0
+
+
+def test_batch_full_4096_matrix_list(cuda):
+    """The batched configuration at its full size: the 4096 matrices of seed
+    1 (sides log-uniform in [16, 4096], widths 1/2/4/8 bytes, AoS->ASTA with
+    tiles 16/32/64 or the full transpose; 9.4 GB) in one arena, converted by
+    one batch call and by a CUDA-graph replay of the same list, every job
+    compared with the oracle each time."""
+    import torch
+    import bench
+    from libmarshal_gb300 import lm
+    from oracle import check as C
+    specs = bench.batch_specs(n=4096)
+    offs, tot = [], 0
+    vjobs = []
+    for op, d, e in specs:
+        code = C.OP_AOS_ASTA if op == "aos_asta" else C.OP_TRANSPOSE
+        offs.append(tot)
+        vjobs.append((tot, code, d, e))
+        tot += (C.n_elems(code, d) * e + 255) // 256 * 256
+    arena = torch.empty(tot, dtype=torch.uint8, device=cuda)
+    base = arena.data_ptr()
+    jobs = [lm.Job(base + off, e, code, *(list(d) + [0] * (4 - len(d))))
+            for (off, code, d, e) in vjobs]
+    bt = lm.Batch()
+
+    def fill_run_check(graph):
+        host = np.empty(tot, dtype=np.uint8)
+        C.fill_host(host, vjobs, 4 << 20)
+        arena.copy_(torch.from_numpy(host))
+        del host
+        bt.run(jobs, graph=graph)
+        torch.cuda.synchronize()
+        bad = C.check_host(arena.cpu().numpy(), vjobs, 4 << 20)
+        assert not bad, ("graph" if graph else "batched", bad[:10])
+
+    fill_run_check(False)
+    bt.run(jobs, graph=True)  # first run of the list with graphs on
+    bt.run(jobs, graph=True)  # second: captured into a graph
+    fill_run_check(True)      # later runs replay it
+    bt.close()
+    assert lm.lib().lm_device_status(None) == 0
+    del arena
+    torch.cuda.empty_cache()

@@ -96,3 +96,30 @@ def test_cycles_cached_leaders_across_streams(cuda):
     torch.cuda.synchronize()
     for buf, w in zip(bufs, want):
         assert np.array_equal(buf.cpu().numpy().view(O.DTYPES[e]), w)
+
+
+def test_soa_asta_full_size_2p27x4_int32(cuda):
+    """The SoA->ASTA configuration at its full size: 2^27 records of 4 int32
+    fields (2 GiB), tile 32, i.e. 100(4, 2^22, 32), through the reference's
+    drop-in entry point, against the oracle's cpu_soa_asta over all host
+    threads; then back (ASTA->SoA) to the input."""
+    import os
+    import torch
+    from libmarshal_gb300 import lm
+    h, w, t = 1 << 27, 4, 32
+    src = O.random_bits(h * w, 4, 2027)
+    want = np.empty_like(src)
+    assert O.lib().lmo_soa_asta_mt(src.ctypes.data, want.ctypes.data, h, w,
+                                   t, 4, os.cpu_count() or 1) == 0
+    buf = torch.from_numpy(src.view(np.int32)).to(cuda)
+    assert not lm.lib().gpu_soa_asta_pttwac(buf.data_ptr(), h, w, t, None), \
+        lm.last_error()
+    torch.cuda.synchronize()
+    assert np.array_equal(buf.cpu().numpy().view(np.uint32), want)
+    del want
+    lm.transpose_100(buf, h // t, w, t, elem_bytes=4)  # ASTA -> SoA
+    torch.cuda.synchronize()
+    assert np.array_equal(buf.cpu().numpy().view(np.uint32), src)
+    assert lm.lib().lm_device_status(None) == 0
+    del buf
+    torch.cuda.empty_cache()
