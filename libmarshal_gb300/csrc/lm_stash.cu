@@ -172,7 +172,11 @@ __global__ void __launch_bounds__(1024) k_stash_offsets(StashArgs sa) {
 
 // K1: copy every row's stash suffix: one warp per row at a time, 16-byte
 // vectors between the (equally misaligned) buffer and stash addresses, the
-// ragged head and tail bytes one by one.  In two passes: first the part of
+// ragged head and tail bytes one by one.  (Splitting the stash into equal
+// contiguous ranges per warp balances the work but ran 30-60 % slower: the
+// warps' streams then sit a fixed distance apart in memory, while suffixes
+// of different lengths keep them staggered; this form runs at the speed of
+// a plain copy of the same bytes.)  In two passes: first the part of
 // each suffix that the wave reads after its first jcut steps, with
 // evict-first stores, then the part those steps read (their strips, about
 // 30 MB for the fp32 16384 x 12289 transposition), with evict-last stores,
@@ -601,9 +605,17 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
       em && atoi(em) > 0 && atoi(em) < 64 ? (uint32_t)atoi(em) : kStashMargin;
   const int per_sms[2] = {ep && atoi(ep) == 1 ? 1 : 2, 1};
   constexpr uint64_t kStepBytes = 40 * 1024;
+  // rows per chunk rounded up so that every chunk's piece of an output row
+  // starts on a 32-byte sector (W*U a multiple of 32), where that keeps 95 %
+  // of the CTAs: a sector is then written by one CTA, not two at different
+  // times (fp32 16384 x 12289: 56 rows instead of 54, wave 3.5 us faster)
+  uint64_t walign = 32;
+  for (uint64_t u = U; u % 2 == 0 && walign > 1; u /= 2) walign /= 2;
   auto try_plan = [&](uint64_t strip, int per_sm) -> bool {
     const uint64_t ctas = (uint64_t)di.sms * per_sm;
-    const uint64_t W = (A + ctas - 1) / ctas;
+    uint64_t W = (A + ctas - 1) / ctas;
+    const uint64_t Wal = (W + walign - 1) / walign * walign;
+    if ((A + Wal - 1) / Wal * 100 >= ctas * 95) W = Wal;
     uint64_t g = std::max<uint64_t>(1, strip / U);
     if (g > B) g = B;
     const uint64_t G = (B + g - 1) / g;
