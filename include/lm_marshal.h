@@ -20,8 +20,20 @@
  *     and adds its GPU time in nanoseconds to *et (the reference's
  *     Profiling::Report, include/cl_profile.h:23-25), and padding/unpadding
  *     always wait in order to read their status word;
- *   - scratch (done bits) comes from the device's stream-ordered memory
- *     pool on the caller's stream; calls on different streams never share it.
+ *   - "in place" means the array's pointer does not change; the planner may
+ *     take device scratch from the device's stream-ordered memory pool on
+ *     the caller's stream (calls on different streams never share it):
+ *       cycle following (PTTWAC): one done bit per unit (a 16384 x 12289
+ *         fp32 transpose: 786 KB);
+ *       the stash plan (100 on units under 128 bytes, e.g. the plain
+ *         transpose of a large matrix): the stash, about half the payload
+ *         (421 MB for 16384 x 12289 fp32), plus 8 bytes per row;
+ *       the staged form (blocks transposed out of place, then copied back):
+ *         the payload's size plus 16 bytes;
+ *       padding: 8 bytes per 4096-element task.
+ *     When the pool cannot supply the stash or the staged form's scratch
+ *     the planner falls through to a method that needs less (ultimately
+ *     cycle following); lm_transpose_100_noalloc allocates nothing.
  *
  * Notation: 010  [A][a][B]     -> [A][B][a]
  *           100  [A][B][b]     -> [B][A][b]
@@ -132,8 +144,11 @@ bool lm_unpadding(lm_stream_t stream, void *buf, int elem_bytes, int x_size,
  * error.  All calls on a
  * device share that array (each clears what it uses first): calls that
  * overlap on the GPU race -- order them on one stream.  The first call on a
- * device looks the array up (with that device current); make it before any
- * stream capture.  Asynchronous, stream ordered; false on success. */
+ * device sets it up (looks the array up with that device current, loads the
+ * kernel's variants, clears one word of the array on `stream`); a call with
+ * zero sizes (e.g. A = B = b = 0, buf NULL) does only that: make one at
+ * start-up, before allocation is forbidden and before any stream capture.
+ * Asynchronous, stream ordered; false on success. */
 bool lm_transpose_100_noalloc(lm_stream_t stream, void *buf, int elem_bytes,
                               int A, int B, int b);
 

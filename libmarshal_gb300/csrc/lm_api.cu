@@ -364,11 +364,14 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
       sp = StashPlan();
     uint32_t *status = sp.feasible ? device_status_word() : nullptr;
     if (sp.feasible && status) {
+      // the stash (about half the payload) may not be available: then the
+      // plans below, which need less scratch, take over
       Scratch sc;
-      if (get_scratch(sc, stash_scratch_bytes(sp), s)) return true;
-      return check_launch(launch_stash100(s, buf, e, a, B, (uint32_t)b, sp,
-                                          sc.p, status, wait_timeout_ns()),
-                          "stash launch");
+      if (try_scratch(sc, stash_scratch_bytes(sp), s))
+        return check_launch(launch_stash100(s, buf, e, a, B, (uint32_t)b, sp,
+                                            sc.p, status, wait_timeout_ns()),
+                            "stash launch");
+      if (m == Method::Stash) return fail("stash: no scratch for this size");
     }
     if (m == Method::Stash)
       return fail("stash plan not applicable to 0100(%llu, %llu, %llu, %llu)",

@@ -1224,6 +1224,8 @@ struct lm_batch_st {
   cudaEvent_t join[lm::kSideStreams] = {};
   cudaEvent_t fork = nullptr, fork2 = nullptr;
   uint64_t seen_key = 0;  // job list of the previous graph-mode run
+  std::vector<lm_job> gjobs, seen_jobs;  // the lists behind gkey / seen_key
+  unsigned gflags = 0, seen_flags = 0;
   // last run statistics
   lm_batch_stats stats;
   int device = -1;
@@ -1231,14 +1233,39 @@ struct lm_batch_st {
 
 using namespace lm;
 
-static uint64_t hash_jobs(const lm_job *jobs, int n) {
+// Key of a job list and its flags (field by field); a key match is
+// confirmed by same_jobs against the kept copy before a graph is replayed.
+static uint64_t hash_jobs(const lm_job *jobs, int n, unsigned flags) {
   uint64_t h = 1469598103934665603ull;
-  const unsigned char *p = reinterpret_cast<const unsigned char *>(jobs);
-  for (size_t i = 0; i < (size_t)n * sizeof(lm_job); ++i) {
-    h ^= p[i];
-    h *= 1099511628211ull;
+  auto mix = [&](uint64_t v) {
+    for (int k = 0; k < 8; ++k) {
+      h ^= (v >> (8 * k)) & 0xff;
+      h *= 1099511628211ull;
+    }
+  };
+  mix(flags);
+  mix((uint64_t)n);
+  for (int i = 0; i < n; ++i) {
+    mix((uint64_t)(uintptr_t)jobs[i].buf);
+    mix((uint64_t)(uint32_t)jobs[i].elem_bytes | ((uint64_t)(uint32_t)jobs[i].op << 32));
+    mix((uint64_t)jobs[i].d0);
+    mix((uint64_t)jobs[i].d1);
+    mix((uint64_t)jobs[i].d2);
+    mix((uint64_t)jobs[i].d3);
   }
-  return h ^ (uint64_t)n;
+  return h;
+}
+
+static bool same_jobs(const std::vector<lm_job> &kept, const lm_job *jobs,
+                      int n) {
+  if (kept.size() != (size_t)n) return false;
+  for (int i = 0; i < n; ++i) {
+    const lm_job &a = kept[i], &b = jobs[i];
+    if (a.buf != b.buf || a.elem_bytes != b.elem_bytes || a.op != b.op ||
+        a.d0 != b.d0 || a.d1 != b.d1 || a.d2 != b.d2 || a.d3 != b.d3)
+      return false;
+  }
+  return true;
 }
 
 // A captured graph holds the device addresses of the tables and the arena:
@@ -1247,6 +1274,7 @@ static void drop_graph(lm_batch_t bt) {
   if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
   bt->gexec = nullptr;
   bt->gkey = 0;
+  bt->gjobs.clear();
 }
 
 // Grows the device tables, the arena and the pinned staging buffer.  Device
@@ -1890,7 +1918,7 @@ static bool launch_t010(cudaStream_t s, const BJob *d_jobs,
   g.counter = counter;
   g.status = nullptr;
   g.stage_bytes = stage;
-  ProfScope ps(s, "batch_tile010");
+  ProfScope ps(s, form_b ? "batch_tile010b" : "batch_tile010");
   kern<<<grid, kBatchThreads, smem, s>>>(g);
   if (cudaGetLastError() != cudaSuccess) return set_error("batch: launch");
   return false;
@@ -2188,15 +2216,17 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
   if (njobs < 0 || (njobs > 0 && !jobs)) return set_error("batch: bad job list");
   cudaStream_t s = (cudaStream_t)stream;
   if (flags & LM_BATCH_GRAPH) {
-    const uint64_t key = hash_jobs(jobs, njobs);
-    if (bt->gexec && key == bt->gkey) {
+    const uint64_t key = hash_jobs(jobs, njobs, flags);
+    if (bt->gexec && key == bt->gkey && flags == bt->gflags &&
+        same_jobs(bt->gjobs, jobs, njobs)) {
       if (cudaGraphLaunch(bt->gexec, s) != cudaSuccess)
         return set_error("batch: graph launch");
       bt->last_stream = s;
       bt->used = true;
       return false;
     }
-    if (key == bt->seen_key) {
+    if (key == bt->seen_key && flags == bt->seen_flags &&
+        same_jobs(bt->seen_jobs, jobs, njobs)) {
       // second run of this job list: record it (everything it touches was
       // initialised by the first run, outside any capture, and the tuned
       // plans are cached), then replay
@@ -2239,6 +2269,8 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
         return set_error("batch: graph instantiate");
       }
       bt->gkey = key;
+      bt->gjobs.assign(jobs, jobs + njobs);
+      bt->gflags = flags;
       if (cudaGraphLaunch(bt->gexec, s) != cudaSuccess)
         return set_error("batch: graph launch");
       bt->last_stream = s;
@@ -2246,6 +2278,8 @@ bool lm_batch_run(lm_batch_t bt, lm_stream_t stream, const lm_job *jobs,
       return false;
     }
     bt->seen_key = key;
+    bt->seen_jobs.assign(jobs, jobs + njobs);
+    bt->seen_flags = flags;
   }
   if (plan_batch(bt, jobs, njobs, flags)) return true;
   return enqueue_batch(bt, s, jobs, flags, nullptr);

@@ -98,6 +98,10 @@ size_t pttwac_flag_bytes(const void *buf, uint64_t T, uint32_t a, uint32_t B,
 cudaError_t launch_pttwac0100(cudaStream_t s, void *buf, int e, uint64_t T,
                               uint32_t a, uint32_t B, uint32_t b,
                               uint32_t *flags);
+// Queries (and so loads, where modules load lazily) every variant of the
+// kernel behind launch_pttwac0100 on the current device, so that later
+// launches do no first-use work.
+cudaError_t pttwac_prepare();
 
 // ---- 010 by in-tile cycle following with done-bits in shared memory ------
 // [A][a][B] -> [A][B][a].  R is the spreading factor of the done-bit map

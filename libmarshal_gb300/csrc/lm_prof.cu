@@ -46,11 +46,12 @@ ProfScope::ProfScope(cudaStream_t s, const char *name) : s_(s), name_(name) {
   // launches recorded into a graph are not timed (their events would
   // belong to the graph, not to a run of it)
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess ||
-      cs != cudaStreamCaptureStatusNone) {
-    cudaGetLastError();
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();  // the query's own error only
     return;
   }
+  if (cs != cudaStreamCaptureStatusNone) return;  // a pending launch error
+                                                  // stays for the caller
   std::lock_guard<std::mutex> lock(g_mu);
   a_ = take_event();
   b_ = take_event();

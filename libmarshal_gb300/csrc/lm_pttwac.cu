@@ -19,12 +19,16 @@
 //  * units larger than 4 KiB are split into independent slices, each with
 //    its own done bits (every slice follows the same cycles);
 //  * data moves through L2 only (ld/st .cg); the claim is an atomicOr whose
-//    returned old value decides the store (control dependency);
-//  * the start of a walk reads its unit *before* checking the unit's bit.
-//    The bit check's address carries a data dependency on every lane's
-//    loaded value (AND with a runtime zero), so the check cannot be performed
-//    before the data has arrived -- otherwise a concurrent claimer could
-//    overwrite the unit between our check and our load.
+//    returned old value decides the store;
+//  * claim and start are the two sides of a message-passing pattern on each
+//    unit: a claimer sets the unit's bit and then overwrites the unit, a
+//    starter reads the unit and then checks the bit.  The claimer's lanes
+//    store only after a warp barrier and a gpu-scope fence that follow the
+//    atomicOr (a release); the starter's lanes fence after their data loads
+//    (an acquire) before the warp barrier after which the leader reads the
+//    bit.  So a starter that finds the bit clear read the unit before any
+//    claimer wrote it -- otherwise a concurrent claimer could overwrite the
+//    unit between our load and our check.
 //  There are no waits: every step either claims a fresh bit or stops, so each
 //  walk ends after at most A*B steps.
 #include <algorithm>
@@ -49,7 +53,6 @@ struct PttArgs {
   uint32_t slice_bytes;
   uint32_t last_slice_bytes;
   uint32_t *flags;
-  uint32_t zero;         // always 0; opaque to the compiler
 };
 
 template <typename VT, int K>
@@ -118,28 +121,27 @@ __global__ void __launch_bounds__(256) k_pttwac(PttArgs g, int logL) {
       const uint32_t off = (uint32_t)(glane + c * L) * VB;
       if (active && off < slen) tmp[c] = __ldcg(reinterpret_cast<const VT *>(uptr + off));
     }
-    uint32_t dep = 0;
     if (__any_sync(kFull, starting)) {
-      // Make the start check depend on the data that was just loaded.
-      if (starting) {
-#pragma unroll
-        for (int c = 0; c < K; ++c) {
-          const uint32_t off = (uint32_t)(glane + c * L) * VB;
-          if (off < slen) dep |= low_word(tmp[c]) & g.zero;
-        }
-      }
-      for (int o = 1; o < L; o <<= 1) dep |= __shfl_xor_sync(kFull, dep, o);
+      // acquire: every lane's data loads before the leader's start check
+      if (starting) __threadfence();
+      __syncwarp();
     }
     const uint64_t f = fbase + pos;
     const uint32_t bit = 1u << (uint32_t)(f & 31);
     uint32_t old = 0;
     if (glane == 0 && active) {
-      uint32_t *wp = g.flags + (f >> 5) + dep;
+      uint32_t *wp = g.flags + (f >> 5);
       old = walking ? atomicOr(wp, bit) : ld_relaxed_gpu(wp);
     }
     old = __shfl_sync(kFull, old, leader);
     const bool hit = (old & bit) != 0;
-    if (active && walking && !hit) {
+    const bool claimed = active && walking && !hit;
+    if (__any_sync(kFull, claimed)) {
+      // release: the leader's claim before every lane's data stores
+      __syncwarp();
+      if (claimed) __threadfence();
+    }
+    if (claimed) {
 #pragma unroll
       for (int c = 0; c < K; ++c) {
         const uint32_t off = (uint32_t)(glane + c * L) * VB;
@@ -216,17 +218,30 @@ size_t pttwac_flag_bytes(const void *buf, uint64_t T, uint32_t a, uint32_t B,
   return (size_t)((sh.total + 31) / 32) * 4;
 }
 
+// CTAs per SM of k_pttwac<VT, K> on the current device, queried once (the
+// query also loads the kernel where modules load lazily).
 template <typename VT, int K>
-static cudaError_t run_ptt(cudaStream_t s, const PttArgs &g, int logL) {
+static cudaError_t ptt_occupancy(int *out) {
   const DeviceInfo &di = device_info();
   static int occ_cache[64] = {0};
   int &occ = occ_cache[di.device & 63];
   if (occ == 0) {
+    int o = 0;
     cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &occ, k_pttwac<VT, K>, 256, 0);
+        &o, k_pttwac<VT, K>, 256, 0);
     if (err != cudaSuccess) return err;
-    if (occ < 1) occ = 1;
+    occ = o < 1 ? 1 : o;
   }
+  *out = occ;
+  return cudaSuccess;
+}
+
+template <typename VT, int K>
+static cudaError_t run_ptt(cudaStream_t s, const PttArgs &g, int logL) {
+  const DeviceInfo &di = device_info();
+  int occ = 0;
+  cudaError_t oerr = ptt_occupancy<VT, K>(&occ);
+  if (oerr != cudaSuccess) return oerr;
   const uint64_t L = 1ull << logL;
   const uint64_t need = (g.total * L + 255) / 256;
   uint64_t blocks = (uint64_t)di.sms * occ;
@@ -252,6 +267,25 @@ static cudaError_t run_ptt_k(cudaStream_t s, const PttArgs &g, int logL,
   }
 }
 
+template <typename VT>
+static cudaError_t ptt_prepare_vt() {
+  int occ = 0;
+  cudaError_t err;
+  if ((err = ptt_occupancy<VT, 1>(&occ)) != cudaSuccess) return err;
+  if ((err = ptt_occupancy<VT, 2>(&occ)) != cudaSuccess) return err;
+  if ((err = ptt_occupancy<VT, 4>(&occ)) != cudaSuccess) return err;
+  return ptt_occupancy<VT, 8>(&occ);
+}
+
+cudaError_t pttwac_prepare() {
+  cudaError_t err;
+  if ((err = ptt_prepare_vt<uint4>()) != cudaSuccess) return err;
+  if ((err = ptt_prepare_vt<uint2>()) != cudaSuccess) return err;
+  if ((err = ptt_prepare_vt<unsigned int>()) != cudaSuccess) return err;
+  if ((err = ptt_prepare_vt<unsigned short>()) != cudaSuccess) return err;
+  return ptt_prepare_vt<unsigned char>();
+}
+
 cudaError_t launch_pttwac0100(cudaStream_t s, void *buf, int e, uint64_t T,
                               uint32_t a, uint32_t B, uint32_t b,
                               uint32_t *flags) {
@@ -273,7 +307,6 @@ cudaError_t launch_pttwac0100(cudaStream_t s, void *buf, int e, uint64_t T,
   g.slice_bytes = sh.slice;
   g.last_slice_bytes = sh.last;
   g.flags = flags;
-  g.zero = 0;
   switch (sh.VB) {
     case 16: return run_ptt_k<uint4>(s, g, sh.logL, sh.K);
     case 8: return run_ptt_k<uint2>(s, g, sh.logL, sh.K);
@@ -294,7 +327,6 @@ struct Ptt010Args {
   uint32_t nwords;       // R * ceil(aB/32)
   uint32_t P;            // padding words per 32
   uint32_t padded_words;
-  uint32_t zero;
 };
 
 template <int E>
@@ -318,9 +350,10 @@ __global__ void __launch_bounds__(1024) k_pttwac010(Ptt010Args g) {
       w += (w >> 5) * g.P;
       if ((done[w] >> bq) & 1u) continue;
       T data = __ldcg(t + i);
-      const uint32_t dep = (uint32_t)data & g.zero;
-      // volatile read after the data has arrived (address dependency)
-      if ((reinterpret_cast<volatile uint32_t *>(done)[w + dep] >> bq) & 1u)
+      // the start check after the data load (acquire at CTA scope: every
+      // claimer of this tile is a thread of this CTA)
+      __threadfence_block();
+      if ((reinterpret_cast<volatile uint32_t *>(done)[w] >> bq) & 1u)
         continue;
       while (true) {
         const T backup = __ldcg(t + pos);
@@ -329,6 +362,7 @@ __global__ void __launch_bounds__(1024) k_pttwac010(Ptt010Args g) {
         pw += (pw >> 5) * g.P;
         const uint32_t old = atomicOr(&done[pw], 1u << pb);
         if ((old >> pb) & 1u) break;
+        __threadfence_block();  // release: the claim before the store
         __stcg(t + pos, data);
         data = backup;
         q = fdiv(pos, g.divB);
@@ -370,7 +404,6 @@ cudaError_t launch_pttwac010_smem(cudaStream_t s, void *buf, int e,
   g.padded_words = ptt010_words(a, B, R, P, &g.nwords);
   g.divWords = make_fastdiv(g.nwords);
   g.P = (uint32_t)P;
-  g.zero = 0;
   const size_t smem = (size_t)g.padded_words * 4;
   const DeviceInfo &di = device_info();
   cudaError_t err = cudaSuccess;

@@ -220,7 +220,11 @@ def test_batch_vector_tile_items(cuda):
     finally:
         lm.prof_enable(False)
     ran = lm.prof_collect()
+    # form A (AoS->ASTA: whole-vector output rows) and form B (ASTA->AoS
+    # specs such as 11 x 64 bytes, 7 x 32 x 4 and 3 x 32 x 2: whole-vector
+    # input rows) both ran
     assert "batch_tile010" in ran, ran
+    assert "batch_tile010b" in ran, ran
     assert st["small_jobs"] > 0
 
 

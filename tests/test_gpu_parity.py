@@ -516,3 +516,24 @@ def test_010_unaligned_buffers(L, e):
         torch.cuda.synchronize()
         got = view.cpu().numpy().view(O.DTYPES[e])
         assert np.array_equal(got, O.t010(src, T, a, B)), (T, a, B, e)
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_pttwac_walkers_racing_in_long_cycles(L, e):
+    """Cycle following (method 2) where nearly every walker starts inside the
+    same few long cycles at once: small A*B (one walker per position, all
+    launched together), shapes with long cycles, units of one to many
+    elements, several tiles; repeated, since the claim and start races are
+    timing dependent.  Bit-exact against the oracle every time."""
+    shapes = [(1, 3, 5, 1), (1, 7, 11, 1), (1, 13, 17, 3), (1, 61, 67, 1),
+              (1, 127, 131, 2), (1, 255, 257, 1), (1, 1000, 999, 1),
+              (1, 4, 1023, 8), (1, 1023, 4, 64), (8, 37, 41, 2),
+              (3, 509, 521, 1)]
+    for (T, a, B, b) in shapes:
+        src = O.random_bits(T * a * B * b, e, T + a + B + b)
+        want = O.t0100(src, T, a, B, b)
+        for rep in range(8):
+            d = to_dev(src)
+            L.transpose_0100(d, T, a, B, b, method=2, elem_bytes=e)
+            assert np.array_equal(from_dev(d, e), want), (T, a, B, b, e, rep)
+    assert L.lib().lm_device_status(None) == 0
