@@ -77,15 +77,42 @@ bool lm_aos_asta_pttwac(lm_stream_t stream, void *buf, int elem_bytes,
 bool lm_aos_asta(lm_stream_t stream, void *buf, int elem_bytes, int height,
                  int width, int tile_size, int R);
 
-/* Full in-place transposition [A*a][B*b] -> [B*b][A*a] through the staged
- * elementary transpositions; stages = 2, 22, 3, 32 or 4, anything else the
- * element-wise fallback.  et may be NULL.
- * Reference: cl_transpose, cl_marshal.h:32-33 / cl_marshal.cc:561-776. */
+/* Full in-place transposition [A*a][B*b] -> [B*b][A*a].  Every stage code
+ * of the reference (2, 22, 3, 32, 4, anything else the element-wise
+ * fallback) yields this same layout; this call runs it as one planned 100
+ * (A*a, B*b, 1), which is faster than the staged sequence, and checks the
+ * arguments as the reference does.  lm_transpose_ex with a forced 010
+ * variant runs the staged elementary transpositions themselves.  et may be
+ * NULL.  Reference: cl_transpose, cl_marshal.h:32-33 / cl_marshal.cc:561-776. */
 bool lm_transpose(lm_stream_t stream, void *buf, int elem_bytes, int A, int a,
                   int B, int b, int R, int stages, unsigned long long *et);
-/* Same with the variant of every 010 step forced: 0 = as lm_transpose (BS when
- * the tile fits on chip, else PTTWAC), 1 = BS, 2 = PTTWAC.  No reference
- * counterpart (the reference picks by MAX_MEM, cl_marshal.cc:578-585). */
+/* Full in-place transposition of an arbitrary M x N matrix ([M][N] ->
+ * [N][M]) by the reference's flow for general matrices
+ * (test/cl_unittest.cc:396-640): "Algorithm 5" chooses the super-element
+ * sizes a and b as the largest divisors in [24, floor(sqrt(MAX_MEM))] of M
+ * and N, each padded by the fewest elements that give it one, "Algorithm 3"
+ * the stage code; then padding (cl_padding) -> the staged transposition
+ * (cl_transpose) -> unpadding (cl_unpadding).  MAX_MEM is the reference's
+ * 48 KB of local memory in elements: 12288 (elements of 1-4 bytes) or 6144
+ * (8 bytes).
+ * lm_full_transpose_plan writes {A, a, B, b, pad_h, pad_w, stages} to plan7
+ * (may be NULL) and the elements the padded flow needs, (M + pad_h) *
+ * (N + pad_w), to padded_elems (may be NULL).
+ * lm_full_transpose: buf holds capacity_elems elements, the M x N matrix
+ * first.  variant010 1 or 2 runs the reference's flow with BS or PTTWAC 010
+ * steps and needs capacity_elems >= the padded count; 0 runs the same
+ * permutation as one planned 100(M, N, 1), with no padding (capacity M*N).
+ * The result is [N][M] in the first M*N elements either way.  et may be
+ * NULL.  The reference has this flow in its test, not as a library call. */
+bool lm_full_transpose_plan(int M, int N, int elem_bytes, int *plan7,
+                            long long *padded_elems);
+bool lm_full_transpose(lm_stream_t stream, void *buf, int elem_bytes, int M,
+                       int N, long long capacity_elems, int variant010,
+                       unsigned long long *et);
+/* Same with the variant of every 010 step: 0 = as lm_transpose (one planned
+ * 100), 1 = the stages with BS 010 steps, 2 = the stages with PTTWAC 010
+ * steps.  No reference counterpart (the reference picks by MAX_MEM,
+ * cl_marshal.cc:578-585). */
 bool lm_transpose_ex(lm_stream_t stream, void *buf, int elem_bytes, int A,
                      int a, int B, int b, int R, int stages, int variant010,
                      unsigned long long *et);

@@ -41,6 +41,8 @@ _SIGS = {
     "lm_aos_asta": (_B, [_VP, _VP, _I, _I, _I, _I, _I]),
     "lm_transpose": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I, _I, _ULLP]),
     "lm_transpose_ex": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _I, _I, _I, _ULLP]),
+    "lm_full_transpose_plan": (_B, [_I, _I, _I, _VP, _VP]),
+    "lm_full_transpose": (_B, [_VP, _VP, _I, _I, _I, _LL, _I, _ULLP]),
     "lm_transpose_010_bs": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
     "lm_transpose_010_pttwac": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP, _I, _I]),
     "lm_transpose_100": (_B, [_VP, _VP, _I, _I, _I, _I, _ULLP]),
@@ -159,6 +161,32 @@ def aos_asta(buf, height, width, tile_size, R=1, stream=None, elem_bytes=None):
     p, e = buf_ptr(buf, elem_bytes)
     _check(lib().lm_aos_asta(stream_ptr(stream), p, e, height, width,
                              tile_size, R), "lm_aos_asta")
+
+
+def full_transpose_plan(M, N, elem_bytes):
+    """The reference's Algorithm 5 / Algorithm 3 choice for an M x N matrix:
+    ((A, a, B, b, pad_h, pad_w, stages), elements the padded flow needs)."""
+    plan = (ctypes.c_int * 7)()
+    need = ctypes.c_longlong()
+    _check(lib().lm_full_transpose_plan(M, N, elem_bytes,
+                                        ctypes.cast(plan, ctypes.c_void_p),
+                                        ctypes.byref(need)),
+           "lm_full_transpose_plan")
+    return tuple(plan), need.value
+
+
+def full_transpose(buf, M, N, variant010=0, stream=None, elem_bytes=None,
+                   timed=False):
+    """[M][N] -> [N][M] in place for any M, N (lm_full_transpose); buf may
+    be longer than M*N (the padded flow of variant010 1 or 2 needs
+    full_transpose_plan's element count)."""
+    p, e = buf_ptr(buf, elem_bytes)
+    cap = buf.numel() * buf.element_size() // e if hasattr(buf, "numel") \
+        else M * N
+    t = _Timer(timed)
+    _check(lib().lm_full_transpose(stream_ptr(stream), p, e, M, N, cap,
+                                   variant010, t.arg()), "lm_full_transpose")
+    return t.ns()
 
 
 def transpose(buf, A, a, B, b, R=1, stages=3, variant010=0, stream=None,

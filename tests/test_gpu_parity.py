@@ -537,3 +537,33 @@ def test_pttwac_walkers_racing_in_long_cycles(L, e):
             L.transpose_0100(d, T, a, B, b, method=2, elem_bytes=e)
             assert np.array_equal(from_dev(d, e), want), (T, a, B, b, e, rep)
     assert L.lib().lm_device_status(None) == 0
+
+
+def test_full_transpose_reference_suite(L):
+    """lm_full_transpose on the reference's `full` suite (15 seeded general
+    matrices, h and w in [1000, 20000), single precision): the reference's
+    flow -- Algorithm 5 padding, the Algorithm 3 staged transposition with
+    BS 010 steps, unpadding -- and the direct form (one planned 100), and on
+    the five smallest shapes the flow with PTTWAC 010 steps; each against the
+    oracle's transpose (all host threads)."""
+    import torch
+    from tests.test_oracle import full_suite_shapes
+    shapes = full_suite_shapes()
+    small = sorted(shapes, key=lambda s: s[0] * s[1])[:5]
+    for n, (M, N) in enumerate(shapes):
+        src = O.random_bits(M * N, 4, 300 + n)
+        want = np.empty_like(src)
+        O.lib().lmo_soa_asta_mt(src.ctypes.data, want.ctypes.data, N, M, 1, 4,
+                                os.cpu_count() or 1)
+        (plan, need) = L.full_transpose_plan(M, N, 4)
+        for variant in ((1, 2) if (M, N) in small else (1,)) + (0,):
+            d = torch.empty(need if variant else M * N, dtype=torch.int32,
+                            device="cuda")
+            d[:M * N].copy_(torch.from_numpy(src.view(np.int32)))
+            L.full_transpose(d, M, N, variant010=variant)
+            torch.cuda.synchronize()
+            got = d[:M * N].cpu().numpy().view(np.uint32)
+            assert np.array_equal(got, want), (M, N, plan, variant)
+            del d
+        torch.cuda.empty_cache()
+    assert L.lib().lm_device_status(None) == 0

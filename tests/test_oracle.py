@@ -152,3 +152,38 @@ def test_oracle_rejects_bad_tiles():
     src = O.random_bits(10 * 3, 4, 0)
     with pytest.raises(ValueError):
         O.aos_asta(src, 10, 3, 4)  # 4 does not divide 10
+
+
+def full_suite_shapes():
+    """The reference's `full` test shapes (test/cl_unittest.cc:344-389,
+    single precision, general matrices): srand(n + 1), h = rand() % 19000 +
+    1000, w = rand() % 19000 + 1000, n = 0..14, with the C library's rand()."""
+    import ctypes
+    libc = ctypes.CDLL("libc.so.6")
+    out = []
+    for n in range(15):
+        libc.srand(n + 1)
+        h = libc.rand() % 19000 + 1000
+        w = libc.rand() % 19000 + 1000
+        out.append((h, w))
+    return out
+
+
+def test_library_full_transpose_plan_matches_oracle(built):
+    """lm_full_transpose_plan (the library's Algorithm 5 / Algorithm 3) gives
+    the oracle's super-element sizes, padding and stage code: for the
+    reference's full suite, the PPoPP'14 sizes and seeded shapes, with the
+    single- (12288) and double-precision (6144) local-memory limits."""
+    from libmarshal_gb300 import lm
+    rng = np.random.default_rng(5)
+    shapes = full_suite_shapes() + [(7200, 1800), (1800, 7200), (5100, 2500),
+                                    (16384, 12289), (23, 5), (97, 101)]
+    shapes += [tuple(int(x) for x in rng.integers(1, 30000, 2))
+               for _ in range(40)]
+    for (h, w) in shapes:
+        for e, mm in ((4, 12288), (8, 6144)):
+            A, a, B, b, ph, pw = O.alg5(h, w, mm)
+            plan, need = lm.full_transpose_plan(h, w, e)
+            assert plan == (A, a, B, b, ph, pw, O.alg3(A, a, B, b, mm)), \
+                (h, w, e)
+            assert need == (h + ph) * (w + pw)
