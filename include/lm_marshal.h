@@ -321,6 +321,15 @@ typedef struct {
 unsigned long long lm_launch_count(void);
 void lm_prof_enable(int on);
 int lm_prof_collect(lm_prof_entry *out, int cap);
+/* Instead of lm_prof_collect: the recorded launches one by one, in launch
+ * order, with start and end in ms from the earliest recorded start (launches
+ * on several streams show their overlap); clears the record and returns the
+ * number of launches recorded (up to cap are written). */
+typedef struct {
+  char name[48];
+  double start_ms, end_ms;
+} lm_prof_span;
+int lm_prof_timeline(lm_prof_span *out, int cap);
 
 #ifdef __cplusplus
 }

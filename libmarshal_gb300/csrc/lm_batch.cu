@@ -42,7 +42,8 @@ constexpr uint64_t kDefaultArenaBytes = 1ull << 30;
 // jobs at least this large that the stash plan applies to skip the staged
 // form (the stash moves 3 x payload, the staged form 4 x)
 constexpr uint64_t kStashPreferBytes = 64ull << 20;
-constexpr int kSideStreams = 6;      // streams of the large jobs and groups
+constexpr int kSideStreams = 6;      // streams of the large jobs
+constexpr int kGroupStreams = 8;     // streams of the item groups
 // jobs at least this large that go through scratch run as the planner's
 // staged form on a side stream (measured on the serving trace and the
 // 4096-matrix batch: 4 and 64 MB were both slower)
@@ -1220,8 +1221,14 @@ struct lm_batch_st {
   uint64_t gkey = 0;
   void *h_gstage = nullptr;  // pinned copy of the job table owned by gexec
   cudaEvent_t uploaded = nullptr;  // last upload from h_stage
-  cudaStream_t side[lm::kSideStreams] = {};  // large jobs and groups run here
+  cudaStream_t side[lm::kSideStreams] = {};  // large jobs run here
   cudaEvent_t join[lm::kSideStreams] = {};
+  // the item groups (persistent kernels) run on streams of their own, one
+  // priority level above the large jobs: they must not wait in stream order
+  // behind large jobs, and their CTAs take SMs as the large jobs' blocks
+  // free them
+  cudaStream_t gside[lm::kGroupStreams] = {};
+  cudaEvent_t gjoin[lm::kGroupStreams] = {};
   cudaEvent_t fork = nullptr, fork2 = nullptr;
   uint64_t seen_key = 0;  // job list of the previous graph-mode run
   std::vector<lm_job> gjobs, seen_jobs;  // the lists behind gkey / seen_key
@@ -1980,6 +1987,18 @@ static bool ensure_side(lm_batch_t bt) {
             cudaSuccess)
       return set_error("batch: side stream");
   }
+  // one step above the large jobs' default priority (a server's lanes keep
+  // the levels above that for their own streams)
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  const int prio = least > greatest ? least - 1 : least;
+  for (int k = 0; k < kGroupStreams; ++k) {
+    if (cudaStreamCreateWithPriority(&bt->gside[k], cudaStreamNonBlocking,
+                                     prio) != cudaSuccess ||
+        cudaEventCreateWithFlags(&bt->gjoin[k], cudaEventDisableTiming) !=
+            cudaSuccess)
+      return set_error("batch: group stream");
+  }
   return false;
 }
 
@@ -2030,9 +2049,7 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   const size_t ni = item_count(bt);
   if (grow(bt, s, std::max<size_t>(nj, 1), std::max<size_t>(ni, 1)))
     return true;
-  // the large jobs need no table: they start first, on the side streams
   unsigned used = 0;
-  if (enqueue_large(bt, s, jobs, flags, &used)) return true;
   // stage: jobs, then small items, big items and the cluster groups.  The
   // shared staging buffer is reused only after the previous upload from it
   // has executed.
@@ -2083,7 +2100,12 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
   // The groups are independent: the staged waves (in order, they share the
   // arena), each cluster size and the one-CTA items run on their own
   // streams, forked here from `s` and joined back at the end, so that one
-  // persistent kernel's tail overlaps the others.
+  // persistent kernel's tail overlaps the others.  Launch order matters: the
+  // cluster groups go first, while the SMs are free (a cluster needs all of
+  // its CTA slots free in one GPC at once, which rarely happens once other
+  // kernels' blocks refill SMs as they drain: the 8-CTA group of the
+  // 4096-matrix list then started 5.3 ms late and ran alone at the end),
+  // then the large jobs (no tables needed), then the other groups.
   const size_t off_big = bt->small.size();
   size_t off_band[kBandGroups];
   size_t off = off_big + bt->big.size();
@@ -2096,39 +2118,21 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
     off += bt->wgather[w].size() + bt->wcopy[w].size();
   const size_t off_t010 = off;
   int nq = 0;
-  cudaStream_t q[1 + kBandGroups + 2];
+  cudaStream_t q[kGroupStreams];
   int ngroups = (bt->nwaves > 0) + (!bt->small.empty() || !bt->big.empty()) +
                 (!bt->t010.empty() || !bt->t010b.empty() || !bt->t010f.empty());
   for (int gi = 0; gi < kBandGroups; ++gi) ngroups += !bt->band[gi].empty();
-  if (ngroups > 1) {
+  if (ngroups > 0) {
     if (ensure_side(bt)) return true;
     cudaEventRecord(bt->fork2, s);  // tables uploaded, counters cleared
   }
+  unsigned gused = 0;
   auto next_stream = [&]() -> cudaStream_t {
-    // the first group runs on s itself
-    if (nq == 0) return q[nq++] = s;
-    cudaStream_t side = bt->side[nq - 1];
+    cudaStream_t side = bt->gside[nq];
     cudaStreamWaitEvent(side, bt->fork2, 0);
-    used |= 1u << (nq - 1);
+    gused |= 1u << nq;
     return q[nq++] = side;
   };
-  if (bt->nwaves > 0) {
-    const cudaStream_t ws = next_stream();
-    off = off_waves;
-    for (int w = 0; w < bt->nwaves; ++w) {
-      uint32_t *c = bt->d_counters + (2 + kBandGroups + 2 * w) * kCounterStride;
-      if (launch_staged(ws, bt->d_jobs, bt->d_items + off,
-                        (uint32_t)bt->wgather[w].size(), c, bt->wsmem[w],
-                        false))
-        return true;
-      off += bt->wgather[w].size();
-      if (launch_staged(ws, bt->d_jobs, bt->d_items + off,
-                        (uint32_t)bt->wcopy[w].size(), c + kCounterStride, 0,
-                        true))
-        return true;
-      off += bt->wcopy[w].size();
-    }
-  }
   for (int gi = kBandGroups - 1; gi >= 0; --gi) {
     if (bt->band[gi].empty()) continue;
     const cudaStream_t bs = next_stream();
@@ -2137,6 +2141,24 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
                     bt->d_counters + (2 + gi) * kCounterStride,
                     bt->band_smem[gi], 2 << gi))
       return true;
+  }
+  if (enqueue_large(bt, s, jobs, flags, &used)) return true;
+  if (bt->nwaves > 0) {
+    const cudaStream_t ws0 = next_stream();
+    off = off_waves;
+    for (int w = 0; w < bt->nwaves; ++w) {
+      uint32_t *c = bt->d_counters + (2 + kBandGroups + 2 * w) * kCounterStride;
+      if (launch_staged(ws0, bt->d_jobs, bt->d_items + off,
+                        (uint32_t)bt->wgather[w].size(), c, bt->wsmem[w],
+                        false))
+        return true;
+      off += bt->wgather[w].size();
+      if (launch_staged(ws0, bt->d_jobs, bt->d_items + off,
+                        (uint32_t)bt->wcopy[w].size(), c + kCounterStride, 0,
+                        true))
+        return true;
+      off += bt->wcopy[w].size();
+    }
   }
   if (!bt->small.empty() || !bt->big.empty()) {
     const cudaStream_t ts = next_stream();
@@ -2177,6 +2199,11 @@ static bool enqueue_batch(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
     cudaEventRecord(bt->join[k], bt->side[k]);
     cudaStreamWaitEvent(s, bt->join[k], 0);
   }
+  for (int k = 0; k < kGroupStreams; ++k) {
+    if (!((gused >> k) & 1)) continue;
+    cudaEventRecord(bt->gjoin[k], bt->gside[k]);
+    cudaStreamWaitEvent(s, bt->gjoin[k], 0);
+  }
   return false;
 }
 
@@ -2204,6 +2231,10 @@ void lm_batch_destroy(lm_batch_t bt) {
   for (int k = 0; k < lm::kSideStreams; ++k) {
     if (bt->side[k]) cudaStreamDestroy(bt->side[k]);
     if (bt->join[k]) cudaEventDestroy(bt->join[k]);
+  }
+  for (int k = 0; k < lm::kGroupStreams; ++k) {
+    if (bt->gside[k]) cudaStreamDestroy(bt->gside[k]);
+    if (bt->gjoin[k]) cudaEventDestroy(bt->gjoin[k]);
   }
   if (bt->fork) cudaEventDestroy(bt->fork);
   if (bt->fork2) cudaEventDestroy(bt->fork2);

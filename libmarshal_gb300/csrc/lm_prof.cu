@@ -115,4 +115,40 @@ int lm_prof_collect(lm_prof_entry *out, int cap) {
   return n;
 }
 
+int lm_prof_timeline(lm_prof_span *out, int cap) {
+  std::vector<Rec> recs;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    recs.swap(g_recs);
+  }
+  // the earliest start is the origin: every start event is compared with
+  // the first recorded one (launches on other streams may start earlier)
+  float origin = 0.f;
+  std::vector<float> t0(recs.size(), 0.f), t1(recs.size(), 0.f);
+  for (size_t k = 0; k < recs.size(); ++k) {
+    if (cudaEventSynchronize(recs[k].b) != cudaSuccess ||
+        cudaEventElapsedTime(&t0[k], recs[0].a, recs[k].a) != cudaSuccess ||
+        cudaEventElapsedTime(&t1[k], recs[0].a, recs[k].b) != cudaSuccess) {
+      cudaGetLastError();
+      t0[k] = t1[k] = 0.f;
+    }
+    if (t0[k] < origin) origin = t0[k];
+  }
+  const int n = (int)recs.size();
+  for (int k = 0; k < n && k < cap; ++k) {
+    memset(&out[k], 0, sizeof(out[k]));
+    strncpy(out[k].name, recs[k].name, sizeof(out[k].name) - 1);
+    out[k].start_ms = t0[k] - origin;
+    out[k].end_ms = t1[k] - origin;
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (const Rec &r : recs) {
+      g_free.push_back(r.a);
+      g_free.push_back(r.b);
+    }
+  }
+  return n;
+}
+
 }  // extern "C"

@@ -71,6 +71,7 @@ _SIGS = {
     "lm_device_status": (ctypes.c_uint, [_VP]),
     "lm_prof_enable": (None, [_I]),
     "lm_prof_collect": (_I, [_VP, _I]),
+    "lm_prof_timeline": (_I, [_VP, _I]),
     "gpu_aos_asta_bs_float": (_B, [_VP, _I, _I, _I, _VP]),
     "gpu_aos_asta_bs_double": (_B, [_VP, _I, _I, _I, _VP]),
     "gpu_aos_asta_pttwac": (_B, [_VP, _I, _I, _I, _VP]),
@@ -274,6 +275,22 @@ class ProfEntry(ctypes.Structure):
 def launch_count() -> int:
     """Kernels launched by the library since it was loaded."""
     return int(lib().lm_launch_count())
+
+
+class ProfSpan(ctypes.Structure):
+    """lm_prof_span of include/lm_marshal.h."""
+    _fields_ = [("name", ctypes.c_char * 48), ("start_ms", ctypes.c_double),
+                ("end_ms", ctypes.c_double)]
+
+
+def prof_timeline():
+    """[(kernel, start_ms, end_ms)] of the launches recorded since profiling
+    was enabled (lm_prof_timeline), in launch order."""
+    cap = 1 << 16
+    arr = (ProfSpan * cap)()
+    n = lib().lm_prof_timeline(ctypes.cast(arr, ctypes.c_void_p), cap)
+    return [(arr[i].name.decode(), arr[i].start_ms, arr[i].end_ms)
+            for i in range(min(n, cap))]
 
 
 def prof_enable(on: bool = True) -> None:
