@@ -252,8 +252,20 @@ bool lm_batch_stats_get(lm_batch_t batch, lm_batch_stats *out);
 /* Bytes of the staging arena of this handle (0: LM_BATCH_SCRATCH_MB, whose
  * default is 1024 MiB); applies from the next lm_batch_run. */
 bool lm_batch_set_arena(lm_batch_t batch, unsigned long long bytes);
-/* Autotuner table: entries tuned so far (and loaded from LM_TUNE_FILE). */
+/* Autotuner table: entries tuned so far (and loaded from LM_TUNE_FILE).  The
+ * batch executor's large jobs (and the server's) run the variant tuned for
+ * their shape class -- key (element width, log2 a, log2 B, log2 b, T > 1)
+ * after widening the units -- found by timing every applicable variant
+ * once: the planner's own choice; the staged form with 16, 32 or 64 KB
+ * blocks; whole-cycle moves; the stash plan with the planner's, one or two
+ * CTAs per SM; the two-pass split; cycle following (variants 0..9 in that
+ * order).  lm_tune_variant pins a class's variant (variant >= 0) or reads it
+ * (variant < 0); it returns the class's variant, or -1 if it has none.  No
+ * reference counterpart (the reference's hand tables, cl_marshal.cc:165-241,
+ * 388-465). */
 int lm_tune_entries(void);
+int lm_tune_variant(int elem_bytes, long long T, long long a, long long B,
+                    long long b, int variant);
 
 /* ---- conversion server (no reference counterpart) -------------------------
  * lm_serve_create starts a worker thread on the current device.  Each

@@ -246,6 +246,40 @@ static uint64_t wait_timeout_ns() {
 
 enum class Method { Auto, BS, Pttwac, Stash, TwoPass, Cycles, Staged };
 
+TuneParams &tune_params() {
+  static thread_local TuneParams p;
+  return p;
+}
+
+// A tuned choice: the method, and the variant of it (an index into the
+// table below) in bits 8-15.
+struct TuneVariant {
+  Method m;
+  TuneParams p;
+};
+static const TuneVariant kVariants[] = {
+    {Method::Auto, {}},
+    {Method::Staged, {16u << 10, 0}},
+    {Method::Staged, {0, 0}},            // 32 KB blocks (built-in)
+    {Method::Staged, {64u << 10, 0}},
+    {Method::Cycles, {}},
+    {Method::Stash, {0, 0}},             // the planner's CTAs per SM
+    {Method::Stash, {0, 1}},
+    {Method::Stash, {0, 2}},
+    {Method::TwoPass, {}},
+    {Method::Pttwac, {}},
+};
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+
+// Sets the thread's tuning overrides for the life of the object.
+struct TuneScope {
+  TuneParams saved;
+  explicit TuneScope(const TuneParams &p) : saved(tune_params()) {
+    tune_params() = p;
+  }
+  ~TuneScope() { tune_params() = saved; }
+};
+
 static bool check_launch(cudaError_t e, const char *what) {
   if (e != cudaSuccess) return cuda_fail(e, what);
   return false;
@@ -460,11 +494,15 @@ static void tune_load_locked() {
   if (!f) return;
   FILE *fp = fopen(f, "r");
   if (!fp) return;
-  TuneKey k;
-  int m;
-  while (fscanf(fp, "%d %d %d %d %d %d", &k.e, &k.la, &k.lB, &k.lb, &k.multi,
-                &m) == 6)
-    g_tune[k] = m;
+  // lines "v2 e log2a log2B log2b multi variant"; other lines are skipped
+  char line[256];
+  while (fgets(line, sizeof(line), fp)) {
+    TuneKey k;
+    int m;
+    if (sscanf(line, "v2 %d %d %d %d %d %d", &k.e, &k.la, &k.lB, &k.lb,
+               &k.multi, &m) == 6)
+      g_tune[k] = m;
+  }
   fclose(fp);
 }
 
@@ -473,7 +511,7 @@ static void tune_save_locked(const TuneKey &k, int m) {
   if (!f) return;
   FILE *fp = fopen(f, "a");
   if (!fp) return;
-  fprintf(fp, "%d %d %d %d %d %d\n", k.e, k.la, k.lB, k.lb, k.multi, m);
+  fprintf(fp, "v2 %d %d %d %d %d %d\n", k.e, k.la, k.lB, k.lb, k.multi, m);
   fclose(fp);
 }
 
@@ -497,48 +535,46 @@ static bool method_applies(Method m, int e, uint64_t T, uint64_t a,
   }
 }
 
-static Method tuned_method(cudaStream_t s, int e, uint64_t T, uint64_t a,
-                           uint64_t B, uint64_t b) {
+// The tuned variant (index into kVariants) of a shape class: every variant
+// that applies is timed once on a scratch buffer of the job's shape (after
+// a warm-up run), the fastest is kept, in memory and in LM_TUNE_FILE.
+static int tuned_variant(cudaStream_t s, int e, uint64_t T, uint64_t a,
+                         uint64_t B, uint64_t b) {
   const TuneKey key{e, ilog2(a), ilog2(B), ilog2(b), T > 1 ? 1 : 0};
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     tune_load_locked();
     auto it = g_tune.find(key);
-    if (it != g_tune.end()) return (Method)it->second;
+    if (it != g_tune.end() && it->second >= 0 && it->second < kNumVariants)
+      return it->second;
   }
   const uint64_t bytes = T * a * B * b * (uint64_t)e;
-  Method cand[6];
-  int nc = 0;
-  cand[nc++] = Method::Auto;
-  if (method_applies(Method::Staged, e, T, a, B, b)) cand[nc++] = Method::Staged;
-  if (method_applies(Method::Cycles, e, T, a, B, b)) cand[nc++] = Method::Cycles;
-  if (T == 1 && plan_stash(a, B, (uint32_t)b, e).feasible) cand[nc++] = Method::Stash;
-  if (b * e < 128 && (split_a(a, B, b, e) || split_B(a, B, b, e)))
-    cand[nc++] = Method::TwoPass;
-  cand[nc++] = Method::Pttwac;
   void *tmp = nullptr;
-  Method best = Method::Auto;
+  int best = 0;
   if (cudaMallocAsync(&tmp, bytes, s) == cudaSuccess) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best_ms = 1e30f;
-    for (int i = 0; i < nc; ++i) {
+    for (int i = 0; i < kNumVariants; ++i) {
+      const TuneVariant &v = kVariants[i];
+      if (v.m == Method::TwoPass && b * e >= 128) continue;
+      TuneScope scope(v.p);
       const std::string saved = g_err;
-      if (!method_applies(cand[i], e, T, a, B, b) ||
-          do_0100(s, tmp, e, T, a, B, b, cand[i])) {  // warm-up
+      if (!method_applies(v.m, e, T, a, B, b) ||
+          do_0100(s, tmp, e, T, a, B, b, v.m)) {  // warm-up
         g_err = saved;
         continue;
       }
       cudaEventRecord(e0, s);
-      do_0100(s, tmp, e, T, a, B, b, cand[i]);
+      do_0100(s, tmp, e, T, a, B, b, v.m);
       cudaEventRecord(e1, s);
       cudaEventSynchronize(e1);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
       if (ms < best_ms) {
         best_ms = ms;
-        best = cand[i];
+        best = i;
       }
     }
     cudaEventDestroy(e0);
@@ -546,21 +582,22 @@ static Method tuned_method(cudaStream_t s, int e, uint64_t T, uint64_t a,
     cudaFreeAsync(tmp, s);
   }
   std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_tune[key] = (int)best;
-  tune_save_locked(key, (int)best);
+  g_tune[key] = best;
+  tune_save_locked(key, best);
   return best;
 }
 
 bool run_0100_planned(cudaStream_t s, void *buf, int e, uint64_t T,
                       uint64_t a, uint64_t B, uint64_t b, int tune) {
-  Method m = Method::Auto;
   if (valid_e(e)) widen_units(buf, &e, &b);  // the tuned class is the wide one
   if (tune && valid_e(e) && T > 0 && a > 1 && B > 1 && b > 0 &&
       T * a * B * b * (uint64_t)e >= (1ull << 20)) {
-    m = tuned_method(s, e, T, a, B, b);
-    if (!method_applies(m, e, T, a, B, b)) m = Method::Auto;
+    const TuneVariant &v = kVariants[tuned_variant(s, e, T, a, B, b)];
+    TuneScope scope(v.p);
+    if (method_applies(v.m, e, T, a, B, b))
+      return do_0100(s, buf, e, T, a, B, b, v.m);
   }
-  return do_0100(s, buf, e, T, a, B, b, m);
+  return do_0100(s, buf, e, T, a, B, b, Method::Auto);
 }
 
 static bool do_010_pttwac(cudaStream_t s, void *buf, int e, uint64_t A,
@@ -928,6 +965,26 @@ int lm_tune_entries(void) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   tune_load_locked();
   return (int)g_tune.size();
+}
+
+// Pins (variant >= 0) or reads (variant < 0) the tuned variant of the shape
+// class of 0100(T, a, B, b) on elem_bytes elements; returns the class's
+// variant afterwards, or -1 when it has none (or the arguments are bad).
+int lm_tune_variant(int elem_bytes, long long T, long long a, long long B,
+                    long long b, int variant) {
+  if (!valid_e(elem_bytes) || T <= 0 || a <= 0 || B <= 0 || b <= 0 ||
+      variant >= kNumVariants)
+    return -1;
+  int e = elem_bytes;
+  uint64_t bb = (uint64_t)b;
+  widen_units(nullptr, &e, &bb);  // the class is keyed on the wide unit
+  const TuneKey key{e, ilog2((uint64_t)a), ilog2((uint64_t)B), ilog2(bb),
+                    T > 1 ? 1 : 0};
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  tune_load_locked();
+  if (variant >= 0) g_tune[key] = variant;
+  auto it = g_tune.find(key);
+  return it == g_tune.end() ? -1 : it->second;
 }
 
 // Planner query used by the Python API's IsFeasible(): 1 when the 0100 tile

@@ -1396,6 +1396,10 @@ static void fill_job(BJob &j, const lm_job &jb, const Normalized &nz,
 static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
                        uint64_t *nblk, size_t *stage_bytes) {
   const uint64_t unit = nz.b * (uint64_t)nz.e;
+  // bytes staged per block: the tuned variant of this shape class, if any
+  const uint64_t kStageTileBytes = tune_params().staged_block_bytes
+                                       ? tune_params().staged_block_bytes
+                                       : lm::kStageTileBytes;
   if (unit > kStageTileBytes || nz.a * nz.B * nz.b >= 0xffffffffull)
     return false;
   auto pitch_of = [&](uint64_t sj) {

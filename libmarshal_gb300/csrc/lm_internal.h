@@ -72,6 +72,17 @@ struct LaunchCache {
 int prepare_launch(const void *kern, LaunchCache &c, size_t smem, int threads,
                    cudaError_t *err);
 
+// ---- per-shape-class tuning overrides ---------------------------------------
+// The autotuner (lm_api.cu, run_0100_planned) picks a method and a variant
+// of it per shape class; the variant reaches the plan builders through
+// these thread-local overrides, set only around the tuned call (0: the
+// built-in choice).
+struct TuneParams {
+  uint32_t staged_block_bytes = 0;  // staged form: bytes staged per block
+  int stash_per_sm = 0;             // stash plan: CTAs per SM (1 or 2)
+};
+TuneParams &tune_params();
+
 // ---- planner thresholds (the per-op planner and the batch executor) ------
 // Measured on GB300 with 256 MB matrices: the staged form (4 x payload
 // through scratch) beats cycle following on units below 512 bytes, ties it

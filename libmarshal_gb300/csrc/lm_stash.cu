@@ -603,7 +603,9 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
   const char *em = getenv("LM_STASH_MARGIN");
   const uint32_t margin =
       em && atoi(em) > 0 && atoi(em) < 64 ? (uint32_t)atoi(em) : kStashMargin;
-  const int per_sms[2] = {ep && atoi(ep) == 1 ? 1 : 2, 1};
+  const int tuned = tune_params().stash_per_sm;
+  const int per_sms[2] = {tuned == 1 || (!tuned && ep && atoi(ep) == 1) ? 1 : 2,
+                          1};
   constexpr uint64_t kStepBytes = 40 * 1024;
   // rows per chunk rounded up so that every chunk's piece of an output row
   // starts on a 32-byte sector (W*U a multiple of 32), where that keeps 95 %
@@ -657,7 +659,8 @@ StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
     }
     return false;
   };
-  if (per_sms[0] == 2) {
+  if (tuned == 2 && best_for(2)) return p;  // the tuned variant, if it fits
+  if (per_sms[0] == 2 && !tuned) {
     StashPlan p2;
     if (best_for(2)) p2 = p;
     // two CTAs per SM with strips below 896 bytes: one CTA per SM with

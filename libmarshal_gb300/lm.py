@@ -72,6 +72,7 @@ _SIGS = {
     "lm_prof_enable": (None, [_I]),
     "lm_prof_collect": (_I, [_VP, _I]),
     "lm_prof_timeline": (_I, [_VP, _I]),
+    "lm_tune_variant": (_I, [_I, _LL, _LL, _LL, _LL, _I]),
     "gpu_aos_asta_bs_float": (_B, [_VP, _I, _I, _I, _VP]),
     "gpu_aos_asta_bs_double": (_B, [_VP, _I, _I, _I, _VP]),
     "gpu_aos_asta_pttwac": (_B, [_VP, _I, _I, _I, _VP]),

@@ -270,3 +270,37 @@ def test_batch_full_4096_matrix_list(cuda):
     assert lm.lib().lm_device_status(None) == 0
     del arena
     torch.cuda.empty_cache()
+
+
+def test_batch_tuned_variants(cuda):
+    """The autotuner's variants (the planner's choice; the staged form with
+    16, 32 or 64 KB blocks; whole-cycle moves; the stash plan with the
+    planner's, one or two CTAs per SM; the two-pass split; cycle following)
+    each pinned for its shape class with lm_tune_variant and run through the
+    batch executor's tuned path (jobs of 16 MB or more), bit-exact against
+    the oracle; a variant that does not apply to the shape falls back to the
+    planner.  Then a class with no entry is tuned by timing."""
+    from libmarshal_gb300 import lm
+    lib = lm.lib()
+    shapes = [  # (op, dims, e): staged-form, stash-plan, short-cycle shapes
+        (lm.OP_TRANSPOSE, (3000, 2000), 4),
+        (lm.OP_100, (8000, 600, 1), 4),
+        (lm.OP_SOA_ASTA, (131072 * 32, 4, 32), 4),
+    ]
+    for op, d, e in shapes:
+        if op == lm.OP_TRANSPOSE:
+            T, a, B, b = 1, d[0], d[1], 1
+        elif op == lm.OP_100:
+            T, a, B, b = 1, d[0], d[1], d[2]
+        else:  # SoA -> ASTA: 100(w, h / t, t)
+            T, a, B, b = 1, d[1], d[0] // d[2], d[2]
+        for v in range(10):
+            assert lib.lm_tune_variant(e, T, a, B, b, v) == v
+            run_and_check(cuda, [(op, d, e)], graph=False, reps=1)
+    # an untuned class (2-byte 9000 x 1100 transposition) gets an entry
+    T, a, B, b = 1, 9000, 1100, 1
+    n0 = lib.lm_tune_entries()
+    assert lib.lm_tune_variant(2, T, a, B, b, -1) == -1
+    run_and_check(cuda, [(lm.OP_TRANSPOSE, (a, B), 2)], graph=False, reps=1)
+    assert lib.lm_tune_variant(2, T, a, B, b, -1) >= 0
+    assert lib.lm_tune_entries() == n0 + 1
