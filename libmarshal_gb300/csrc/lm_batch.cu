@@ -80,6 +80,9 @@ struct BJob {
   // pitch, 16-byte pieces per row, rows of a full item and its tiles
   uint32_t tpitch, kt;
   FastDiv div_nc, div_rows;
+  // staged form, b == 1 and 1- or 2-byte elements: staged rows start on
+  // 32-bit words and output vectors on 16 bytes (store_b1_vec applies)
+  uint32_t vb1;
 };
 
 struct BItem {
@@ -558,6 +561,73 @@ __device__ __forceinline__ void store_b1(const unsigned char *buf,
   }
 }
 
+// store_b1 for 1- and 2-byte elements with whole 16-byte output vectors:
+// lane l of a warp takes 32-bit word column w (4/E staged columns) of a
+// group of 16/E staged rows (one word per row: the warp reads 32
+// consecutive words of a row at a time, no bank conflicts), transposes the
+// bytes in registers and writes one 16-byte vector to each of its 4/E
+// output rows.  Staged rows must start on 32-bit words, nrows be a multiple
+// of 16/E, ncols of 4/E, and the vectors dst + jj*ostride + i land on 16
+// bytes (ostride*E and the block's first row a multiple of 16 bytes).
+template <int E>
+__device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
+                                             const uint32_t *rowoff,
+                                             uint32_t nrows, uint32_t ncols,
+                                             typename Elem<E>::T *dst,
+                                             uint32_t ostride, uint32_t warp,
+                                             uint32_t nwarps) {
+  static_assert(E == 1 || E == 2, "narrow elements only");
+  constexpr uint32_t RW = 16 / E;  // staged rows per output vector
+  constexpr uint32_t CW = 4 / E;   // staged columns per 32-bit word
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t ngr = nrows / RW, nwc = ncols / CW;
+  const uint32_t nch = (nwc + 31) / 32;
+  for (uint32_t u = warp; u < ngr * nch; u += nwarps) {
+    const uint32_t g = u / nch, wc = (u - g * nch) * 32 + lane;
+    if (wc >= nwc) continue;
+    const unsigned char *col = buf + wc * 4;
+    const uint32_t r0 = g * RW;
+    auto word = [&](uint32_t k) {
+      return *reinterpret_cast<const uint32_t *>(col + rowoff[r0 + k]);
+    };
+    uint4 out[CW];
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+      uint32_t c[CW];
+      if constexpr (E == 1) {
+        // a 4 x 4 byte transpose: rows 4q..4q+3 into word q of each column
+        const uint32_t a0 = word(4 * q), a1 = word(4 * q + 1),
+                       a2 = word(4 * q + 2), a3 = word(4 * q + 3);
+        const uint32_t lo01 = __byte_perm(a0, a1, 0x5140);
+        const uint32_t hi01 = __byte_perm(a0, a1, 0x7362);
+        const uint32_t lo23 = __byte_perm(a2, a3, 0x5140);
+        const uint32_t hi23 = __byte_perm(a2, a3, 0x7362);
+        c[0] = __byte_perm(lo01, lo23, 0x5410);
+        c[1] = __byte_perm(lo01, lo23, 0x7632);
+        c[2] = __byte_perm(hi01, hi23, 0x5410);
+        c[3] = __byte_perm(hi01, hi23, 0x7632);
+      } else {
+        // 2-byte elements: rows 2q, 2q+1 into word q of each column
+        const uint32_t a0 = word(2 * q), a1 = word(2 * q + 1);
+        c[0] = __byte_perm(a0, a1, 0x5410);
+        c[1] = __byte_perm(a0, a1, 0x7632);
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < CW; ++k) {
+        if (q == 0) out[k].x = c[k];
+        else if (q == 1) out[k].y = c[k];
+        else if (q == 2) out[k].z = c[k];
+        else out[k].w = c[k];
+      }
+    }
+#pragma unroll
+    for (uint32_t c = 0; c < CW; ++c)
+      __stcg(reinterpret_cast<uint4 *>(dst + (uint64_t)(wc * CW + c) * ostride +
+                                       g * RW),
+             out[c]);
+  }
+}
+
 // Tiles larger than one CTA's shared memory, processed by persistent
 // clusters: rank 0 claims items and shares them through distributed shared
 // memory; each CTA stages a column band of the tile with bulk copies
@@ -853,6 +923,13 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
     return;
   }
   if (j.b == 1) {
+    if constexpr (E <= 2) {
+      if (j.vb1 && k.si % (16 / E) == 0 && k.sj % (4 / E) == 0) {
+        store_b1_vec<E>(buf, rowoff, k.si, k.sj, dst, j.a, threadIdx.x >> 5,
+                        kStageThreads / 32);
+        return;
+      }
+    }
     store_b1<E>(buf, rowoff, k.si, k.sj, j.ng8, j.div_ng8, dst, j.a,
                 threadIdx.x >> 5, kStageThreads / 32);
     return;
@@ -892,7 +969,12 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
 // Persistent: every CTA walks blocks (claimed item by item from the work
 // counter) with two shared-memory stages, loading block n+1 by bulk copies
 // while it writes block n.
-__global__ void __launch_bounds__(kStageThreads, 3) k_batch_gather(BatchArgs g) {
+// MB: CTAs per SM the registers are sized for.  Three suit the mixed
+// batches and 1-byte blocks; the vectorized store of 2-byte blocks wants the
+// registers of two (16384 x 16384 2-byte staged transposition: gather 0.358
+// vs 0.436 ms, while 1-byte blocks lose 0.236 -> 0.289 ms).
+template <int MB>
+__global__ void __launch_bounds__(kStageThreads, MB) k_batch_gather(BatchArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t rowoff[2][kStageMaxS];
@@ -1436,6 +1518,13 @@ static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.div_S = make_fastdiv(S);
   j.nv16 = (unit % 16 == 0 && ((uintptr_t)jb.buf & 15) == 0)
                ? (uint32_t)(unit / 16) : 0u;
+  // staged rows on 32-bit words (row length, buffer and block columns) and
+  // output vectors on 16 bytes (output row length and block rows; the
+  // scratch sits at the buffer's address modulo 16)
+  j.vb1 = (nz.b == 1 && nz.e <= 2 && ((uintptr_t)jb.buf & 15) == 0 &&
+           (nz.B * nz.e) % 4 == 0 && (Sj * nz.e) % 4 == 0 &&
+           (nz.a * nz.e) % 16 == 0 && (S * nz.e) % 16 == 0)
+              ? 1u : 0u;
   j.div_nv16 = make_fastdiv(j.nv16 ? j.nv16 : 1);
   j.ng8 = (S + 7) / 8;
   j.div_ng8 = make_fastdiv(j.ng8);
@@ -1767,7 +1856,7 @@ static bool launch_staged(cudaStream_t s, const BJob *d_jobs,
                           uint32_t *counter, size_t smem, bool copyback) {
   if (nitems == 0) return false;
   const DeviceInfo &di = device_info();
-  auto kern = copyback ? k_batch_copyback : k_batch_gather;
+  auto kern = copyback ? k_batch_copyback : k_batch_gather<3>;
   // the gather keeps two stages of `smem` bytes
   const size_t dyn = copyback ? 0 : 2 * smem;
   if (dyn > 48 * 1024 &&
@@ -1835,16 +1924,17 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
   size_t stage = 0;
   if (!staged_job(g.single, jb, nz, &nblk, &stage)) return cudaErrorInvalidValue;
   g.single.scratch = reinterpret_cast<char *>(scratch);
+  auto gather = (e == 2 && g.single.vb1) ? k_batch_gather<2> : k_batch_gather<3>;
   const size_t dyn = 2 * stage;
   cudaError_t err = cudaSuccess;
   if (dyn > 48 * 1024 &&
-      (err = cudaFuncSetAttribute(k_batch_gather,
+      (err = cudaFuncSetAttribute(gather,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)dyn)) != cudaSuccess)
     return err;
   int occ = 0;
   if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-           &occ, k_batch_gather, kStageThreads, dyn)) != cudaSuccess)
+           &occ, gather, kStageThreads, dyn)) != cudaSuccess)
     return err;
   const DeviceInfo &di = device_info();
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
@@ -1857,7 +1947,7 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
   g.stage_bytes = (uint32_t)stage;
   {
     ProfScope ps(s, "staged_gather");
-    k_batch_gather<<<grid, kStageThreads, dyn, s>>>(g);
+    gather<<<grid, kStageThreads, dyn, s>>>(g);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
   if (g.single.bytes > kL2StageBytes ||

@@ -567,3 +567,22 @@ def test_full_transpose_reference_suite(L):
             del d
         torch.cuda.empty_cache()
     assert L.lib().lm_device_status(None) == 0
+
+
+@pytest.mark.parametrize("e", [1, 2])
+def test_staged_narrow_vector_store(L, e):
+    """The staged form (method 6) on 1- and 2-byte one-element units: shapes
+    whose staged rows start on 32-bit words and whose output vectors land on
+    16 bytes take the vectorized transposed store (whole 16-byte output
+    vectors), the others the element-wise one; several tiles, ragged block
+    edges; bit-exact against the oracle."""
+    shapes = [(1, 7200, 1800), (1, 1024, 4000), (3, 256, 1000),
+              (1, 4096, 500), (2, 48, 2000), (1, 7200, 1801),
+              (1, 1000, 1000), (1, 336, 4004), (4, 160, 24)]
+    for (T, a, B) in shapes:
+        src = O.random_bits(T * a * B, e, T + a + B)
+        d = to_dev(src)
+        L.transpose_0100(d, T, a, B, 1, method=6, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), O.t0100(src, T, a, B, 1)), \
+            (T, a, B, e)
+    assert L.lib().lm_device_status(None) == 0
