@@ -132,3 +132,50 @@ def test_serve_rejects_bad_requests(cuda):
     srv.submit(lm.OP_TRANSPOSE, (64, 64), 1, buf=b)
     srv.drain(10000)
     srv.close()
+
+
+def test_serve_poisson_trace_every_request(cuda):
+    """The served configuration's trace generator (Poisson arrivals at 100k
+    requests/s, seed 2, the five layout conversions, widths 1/2/4/8) with
+    400 requests of 4 KiB to 64 MiB, each on its own device region with a
+    seeded input: replayed at its arrival times through the server (in the
+    mix, continuously batched) and one request per call (alone); every
+    request's result against the oracle in both forms."""
+    import torch
+    import bench
+    from libmarshal_gb300 import lm
+    from oracle import check as C
+    trace = bench.serve_trace(400, 100000.0, hi=64 << 20)
+    code = {"aos_asta": C.OP_AOS_ASTA, "asta_aos": C.OP_ASTA_AOS,
+            "soa_asta": C.OP_SOA_ASTA, "asta_soa": C.OP_ASTA_SOA,
+            "transpose": C.OP_TRANSPOSE}
+    offs, tot = [], 0
+    for (_, op, d, e) in trace:
+        offs.append(tot)
+        tot += (C.n_elems(code[op], d) * e + 255) // 256 * 256
+    arena = torch.empty(tot, dtype=torch.uint8, device=cuda)
+    vjobs = [(off, code[op], d, e) for off, (_, op, d, e) in zip(offs, trace)]
+    reqs, arrival = [], []
+    for (t_ns, op, d, e), off in zip(trace, offs):
+        r = lm.Request()
+        r.elem_bytes, r.op = e, code[op]
+        r.d0, r.d1, r.d2, r.d3 = list(d) + [0] * (4 - len(d))
+        r.buf = arena.data_ptr() + off
+        reqs.append(r)
+        arrival.append(t_ns)
+    for mode in ("served", "plain"):
+        host = np.empty(tot, dtype=np.uint8)
+        C.fill_host(host, vjobs, 8 << 20)
+        arena.copy_(torch.from_numpy(host))
+        del host
+        torch.cuda.synchronize()
+        srv = lm.Server(16 << 30) if mode == "served" else None
+        res = lm.serve_replay(srv, reqs, arrival, None,
+                              plain=(mode == "plain"))
+        if srv is not None:
+            srv.close()
+        torch.cuda.synchronize()
+        assert not any(r[0] for r in res), mode
+        bad = C.check_host(arena.cpu().numpy(), vjobs, 8 << 20)
+        assert not bad, (mode, bad[:10])
+    assert lm.lib().lm_device_status(None) == 0
