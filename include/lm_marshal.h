@@ -142,7 +142,11 @@ bool lm_transpose_0100(lm_stream_t stream, void *buf, int elem_bytes, int A,
  * cycles (when every cycle of 100(a, B) has at most 32 units: find each
  * cycle's smallest position, then move whole cycles through registers),
  * 6 = through scratch (each tile's blocks transposed out of place into a
- * stream-ordered scratch buffer of the payload's size, then copied back).  Returns
+ * stream-ordered scratch buffer of the payload's size, then copied back),
+ * 7 = held in shared memory (payloads up to about 30 MB: every CTA loads its
+ * blocks, all CTAs meet at a grid barrier, then write their blocks
+ * transposed over the buffer; one cooperative launch, no scratch; not
+ * under stream capture).  Returns
  * true when the forced algorithm does not apply to the shape.  No reference
  * counterpart (the reference picks by super-element size,
  * cl_marshal.cc:365-370). */

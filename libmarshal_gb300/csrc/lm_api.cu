@@ -244,11 +244,16 @@ static uint64_t wait_timeout_ns() {
 
 // ---- planner ----------------------------------------------------------------
 
-enum class Method { Auto, BS, Pttwac, Stash, TwoPass, Cycles, Staged };
+enum class Method { Auto, BS, Pttwac, Stash, TwoPass, Cycles, Staged, Resident };
 
 TuneParams &tune_params() {
   static thread_local TuneParams p;
   return p;
+}
+
+bool &planner_beside_other_work() {
+  static thread_local bool v = false;
+  return v;
 }
 
 // A tuned choice: the method, and the variant of it (an index into the
@@ -378,6 +383,25 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
       return fail("cycles: the cycles of 100(%llu, %llu) are longer than %u",
                   (unsigned long long)a, (unsigned long long)B,
                   (unsigned)kCycleMaxLen);
+  }
+  // a payload that fits the shared memory of all SMs: one cooperative
+  // launch at 2 x payload (not beside other work, where it would wait for
+  // every SM to drain, nor under stream capture)
+  if (m == Method::Resident ||
+      (m == Method::Auto && !planner_beside_other_work() &&
+       !getenv("LM_NO_RESIDENT"))) {
+    uint32_t *status = device_status_word();
+    const cudaError_t err =
+        status ? launch_resident0100(s, buf, e, T, a, B, b, status,
+                                     wait_timeout_ns())
+               : cudaErrorNotSupported;
+    if (err == cudaSuccess) return false;
+    if (err != cudaErrorNotSupported) return cuda_fail(err, "resident launch");
+    if (m == Method::Resident)
+      return fail("resident: 0100(%llu, %llu, %llu, %llu) does not fit shared "
+                  "memory (or the stream is being captured)",
+                  (unsigned long long)T, (unsigned long long)a,
+                  (unsigned long long)B, (unsigned long long)b);
   }
   // the stash wavefront spreads rows over all CTAs: with too few rows per
   // SM its steps are too small to keep HBM busy
@@ -530,6 +554,8 @@ static bool method_applies(Method m, int e, uint64_t T, uint64_t a,
       return cycle_order(a, B, kCycleMaxLen) != 0 && a * B - 1 <= (1ull << 28);
     case Method::Staged:
       return staged0100_applies(T, a, B, b, e);
+    case Method::Resident:
+      return resident0100_applies(T, a, B, b, e);
     default:
       return true;
   }
@@ -807,13 +833,14 @@ bool lm_transpose_0100_method(lm_stream_t stream, void *buf, int elem_bytes,
                               unsigned long long *et) {
   OpTimer t(et, (cudaStream_t)stream);
   if (A < 0 || a < 0 || B < 0 || b < 0) return fail("dimensions must be >= 0");
-  if (method < 0 || method > 6) return fail("method must be 0..6");
+  if (method < 0 || method > 7) return fail("method must be 0..7");
   const Method m = method == 1   ? Method::BS
                    : method == 2 ? Method::Pttwac
                    : method == 3 ? Method::Stash
                    : method == 4 ? Method::TwoPass
                    : method == 5 ? Method::Cycles
                    : method == 6 ? Method::Staged
+                   : method == 7 ? Method::Resident
                                  : Method::Auto;
   if (do_0100((cudaStream_t)stream, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
               (uint64_t)B, (uint64_t)b, m))

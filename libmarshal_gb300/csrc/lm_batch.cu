@@ -1968,6 +1968,225 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
   return cudaGetLastError();
 }
 
+// ---- 0100 held whole in shared memory ---------------------------------------
+// A payload that fits the shared memory of all SMs together moves in place
+// in one cooperative launch at 2 x payload: every CTA copies its blocks of
+// the staged form's block grid (blocks blockIdx.x + k * gridDim.x) into
+// shared memory, the CTAs meet at a grid barrier (every read of the buffer
+// is done before any write), then each writes its blocks transposed straight
+// over the buffer.  The barrier counts arrivals in one word of a ring that
+// only grows: the host hands every launch a slot and the count that slot
+// reaches when all of the launch's CTAs have arrived, so no word is ever
+// reset (and a captured launch, whose count would be stale on replay, takes
+// the staged form instead).
+constexpr uint32_t kResMaxBlocks = 16;  // blocks one CTA holds
+constexpr uint32_t kResSlots = 1024;
+__device__ uint32_t g_res_arrivals[kResSlots];
+
+struct ResArgs {
+  BJob job;              // the staged form's job, written over itself
+  uint32_t nblk;         // blocks of the job
+  uint32_t nper;         // most blocks of one CTA
+  uint32_t stage_bytes;  // shared-memory bytes of one block
+  uint32_t slot, target;
+  uint32_t *status;
+  uint64_t timeout_ns;
+};
+
+__global__ void __launch_bounds__(kStageThreads, 1) k_resident(ResArgs g) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar[kResMaxBlocks];
+  __shared__ __align__(16) BJob s_job;
+  __shared__ int s_ok;
+  const uint32_t warp = threadIdx.x >> 5, nw = kStageThreads / 32;
+  const uint32_t nmine =
+      g.nblk > blockIdx.x ? (g.nblk - blockIdx.x + gridDim.x - 1) / gridDim.x
+                          : 0;
+  uint32_t *rowoff =
+      reinterpret_cast<uint32_t *>(smem + (size_t)g.nper * g.stage_bytes);
+  if (threadIdx.x == 0) {
+    for (uint32_t k = 0; k < nmine; ++k) mbar_init(&bar[k], 1);
+    fence_mbar_init();
+    s_ok = 1;
+  }
+  if (warp == 0) copy_job(&s_job, &g.job);
+  __syncthreads();
+  // one warp per block issues its row copies
+  for (uint32_t k = warp; k < nmine; k += nw)
+    gather_issue(s_job, blockIdx.x + k * gridDim.x,
+                 smem + (size_t)k * g.stage_bytes, rowoff + k * s_job.S,
+                 &bar[k]);
+  bool landed = true;
+  const uint64_t t0 = global_timer_ns();
+  for (uint32_t k = 0; k < nmine && landed; ++k)
+    while (!mbar_try_wait(&bar[k], 0))
+      if (global_timer_ns() - t0 > g.timeout_ns) {
+        landed = false;
+        break;
+      }
+  if (!landed) s_ok = 0;
+  __syncthreads();
+  // grid barrier: every CTA arrives exactly once, then waits (bounded) for
+  // the slot to reach the launch's target
+  if (threadIdx.x == 0) {
+    uint32_t *ctr = &g_res_arrivals[g.slot];
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    const uint64_t t1 = global_timer_ns();
+    while ((int32_t)(ld_acquire_gpu(ctr) - g.target) < 0) {
+      if (global_timer_ns() - t1 > g.timeout_ns) {
+        s_ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (!s_ok && g.status) atomicExch(g.status, kStatusWaitTimeout);
+  }
+  __syncthreads();
+  if (s_ok) {
+    for (uint32_t k = 0; k < nmine; ++k) {
+      const uint32_t q = blockIdx.x + k * gridDim.x;
+      const unsigned char *buf = smem + (size_t)k * g.stage_bytes;
+      const uint32_t *ro = rowoff + k * s_job.S;
+      switch (s_job.e) {
+        case 1: gather_store<1>(s_job, q, buf, ro); break;
+        case 2: gather_store<2>(s_job, q, buf, ro); break;
+        case 4: gather_store<4>(s_job, q, buf, ro); break;
+        default: gather_store<8>(s_job, q, buf, ro); break;
+      }
+    }
+    return;
+  }
+  // nothing may still be landing in shared memory when the CTA exits
+  const uint64_t t2 = global_timer_ns();
+  for (uint32_t k = 0; k < nmine; ++k)
+    while (!mbar_try_wait(&bar[k], 0) && global_timer_ns() - t2 < g.timeout_ns) {
+    }
+}
+
+namespace {
+
+// Per device: the dynamic shared memory k_resident may take, and the
+// arrivals each barrier slot has been given so far.
+struct ResDevice {
+  size_t max_dyn = 0;
+  uint32_t next = 0;
+  uint32_t arrivals[kResSlots] = {};
+};
+std::mutex g_res_mu;
+ResDevice *g_res_dev[64];
+
+// The block grid of a resident 0100: the largest staged block (32, 16 or
+// 8 KB) whose blocks fit one CTA per SM.
+bool plan_resident(ResArgs &g, uint32_t *grid, size_t *dyn, void *buf,
+                   uint64_t T, uint64_t a, uint64_t B, uint64_t b, int e,
+                   size_t max_dyn) {
+  const DeviceInfo &di = device_info();
+  lm_job jb{};
+  jb.buf = buf;
+  jb.elem_bytes = e;
+  Normalized nz;
+  nz.ok = true;
+  nz.e = e;
+  nz.T = T;
+  nz.a = a;
+  nz.B = B;
+  nz.b = b;
+  if (T * a * B * b * (uint64_t)e > (uint64_t)di.sms * max_dyn) return false;
+  const TuneParams saved = tune_params();
+  bool ok = false;
+  for (uint32_t tb : {32u << 10, 16u << 10, 8u << 10}) {
+    tune_params().staged_block_bytes = tb;
+    uint64_t nblk = 0;
+    size_t stage = 0;
+    if (!staged_job(g.job, jb, nz, &nblk, &stage)) continue;
+    const uint64_t G = std::min<uint64_t>((uint64_t)di.sms, nblk);
+    const uint64_t nper = (nblk + G - 1) / G;
+    const size_t need = nper * stage + (nper * g.job.S * 4 + 15) / 16 * 16;
+    if (nper > kResMaxBlocks || need > max_dyn) continue;
+    g.nblk = (uint32_t)nblk;
+    g.nper = (uint32_t)nper;
+    g.stage_bytes = (uint32_t)stage;
+    *grid = (uint32_t)G;
+    *dyn = need;
+    ok = true;
+    break;
+  }
+  tune_params() = saved;
+  return ok;
+}
+
+// The device's ResDevice, set up on first use (nullptr on failure).
+ResDevice *res_device() {
+  const DeviceInfo &di = device_info();
+  if (di.device < 0 || di.device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_res_mu);
+  ResDevice *d = g_res_dev[di.device];
+  if (d) return d;
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, k_resident) != cudaSuccess) return nullptr;
+  const size_t max_dyn =
+      (size_t)di.max_smem_optin > fa.sharedSizeBytes
+          ? ((size_t)di.max_smem_optin - fa.sharedSizeBytes) / 128 * 128
+          : 0;
+  if (cudaFuncSetAttribute(k_resident,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)max_dyn) != cudaSuccess)
+    return nullptr;
+  d = new ResDevice;
+  d->max_dyn = max_dyn;
+  g_res_dev[di.device] = d;
+  return d;
+}
+
+}  // namespace
+
+bool resident0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
+                          int e) {
+  if (T == 0 || a <= 1 || B <= 1 || b == 0) return false;
+  ResDevice *d = res_device();
+  if (!d) return false;
+  ResArgs g{};
+  uint32_t grid = 0;
+  size_t dyn = 0;
+  return plan_resident(g, &grid, &dyn, nullptr, T, a, B, b, e, d->max_dyn);
+}
+
+cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
+                                uint64_t a, uint64_t B, uint64_t b,
+                                uint32_t *status, uint64_t timeout_ns) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t err = cudaStreamIsCapturing(s, &cs);
+  if (err != cudaSuccess) return err;
+  if (cs != cudaStreamCaptureStatusNone) return cudaErrorNotSupported;
+  ResDevice *d = res_device();
+  if (!d) return cudaErrorNotSupported;
+  ResArgs g{};
+  uint32_t grid = 0;
+  size_t dyn = 0;
+  if (!plan_resident(g, &grid, &dyn, buf, T, a, B, b, e, d->max_dyn))
+    return cudaErrorNotSupported;
+  g.job.scratch = g.job.base;
+  g.status = status;
+  g.timeout_ns = timeout_ns;
+  {
+    std::lock_guard<std::mutex> lock(g_res_mu);
+    g.slot = d->next++ % kResSlots;
+    d->arrivals[g.slot] += grid;
+    g.target = d->arrivals[g.slot];
+  }
+  void *args[] = {&g};
+  ProfScope ps(s, "resident");
+  err = cudaLaunchCooperativeKernel((const void *)k_resident, dim3(grid),
+                                    dim3(kStageThreads), args, dyn, s);
+  if (err != cudaSuccess) {
+    // no CTA arrives: the slot keeps the count it had
+    std::lock_guard<std::mutex> lock(g_res_mu);
+    d->arrivals[g.slot] -= grid;
+  }
+  return err;
+}
+
 }  // namespace lm
 
 static bool launch_small(cudaStream_t s, const BJob *d_jobs,
@@ -2122,6 +2341,12 @@ static bool enqueue_large(lm_batch_t bt, cudaStream_t s, const lm_job *jobs,
     }
   }
   uint64_t load[kSideStreams] = {};
+  // these jobs run beside the batch's kernels
+  struct Beside {
+    bool saved = planner_beside_other_work();
+    Beside() { planner_beside_other_work() = true; }
+    ~Beside() { planner_beside_other_work() = saved; }
+  } beside;
   for (uint32_t k : order) {
     int best = 0;
     for (int q = 1; q < nside; ++q)

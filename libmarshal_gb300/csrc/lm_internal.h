@@ -83,6 +83,11 @@ struct TuneParams {
 };
 TuneParams &tune_params();
 
+// True on a thread while the batch executor runs planner jobs beside its
+// other kernels: the planner then takes no whole-GPU cooperative form (its
+// launch would wait for every SM to drain).
+bool &planner_beside_other_work();
+
 // ---- planner thresholds (the per-op planner and the batch executor) ------
 // Measured on GB300 with 256 MB matrices: the staged form (4 x payload
 // through scratch) beats cycle following on units below 512 bytes, ties it
@@ -176,6 +181,18 @@ bool staged0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b, int e);
 cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
                               uint64_t a, uint64_t B, uint64_t b,
                               void *scratch);
+
+// ---- 0100 held whole in shared memory (lm_batch.cu) -------------------------
+// Payloads that fit the shared memory of all SMs (about 30 MB on GB300): the
+// staged form's blocks loaded by every CTA, a grid barrier, then written
+// transposed over the buffer: one cooperative launch, 2 x payload.
+// cudaErrorNotSupported when the shape does not fit or the stream is being
+// captured.  A barrier wait that runs out sets `status` and skips the writes.
+bool resident0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
+                          int e);
+cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
+                                uint64_t a, uint64_t B, uint64_t b,
+                                uint32_t *status, uint64_t timeout_ns);
 
 // A 0100 moves whole units of b elements, so the same byte permutation is a
 // 0100 over elements of any width w dividing the unit's b*e bytes.  Widens

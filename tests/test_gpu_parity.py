@@ -586,3 +586,62 @@ def test_staged_narrow_vector_store(L, e):
         assert np.array_equal(from_dev(d, e), O.t0100(src, T, a, B, 1)), \
             (T, a, B, e)
     assert L.lib().lm_device_status(None) == 0
+
+
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
+def test_resident_form(L, e):
+    """The shared-memory-resident form (method 7: every CTA loads its blocks,
+    grid barrier, blocks written transposed over the buffer): one- and
+    many-tile shapes, units of one to many elements, ragged block edges,
+    fewer blocks than SMs, a buffer that is only element-aligned; bit-exact
+    against the oracle.  A payload beyond the shared memory of all SMs is
+    refused with the buffer unchanged."""
+    import torch
+    shapes = [(1, 7200, 1800, 1), (1, 1000, 1000, 1), (3, 256, 1000, 1),
+              (1, 4096, 500, 1), (1, 7200, 1801, 1), (5, 100, 90, 3),
+              (1, 33, 65, 7), (2, 2000, 300, 2), (1, 3, 5, 1), (1, 1500, 1700, 1)]
+    for (T, a, B, b) in shapes:
+        n = T * a * B * b
+        if n * e > 24 << 20:
+            continue
+        src = O.random_bits(n, e, T + a + B + b)
+        want = O.t0100(src, T, a, B, b)
+        d = to_dev(src)
+        L.transpose_0100(d, T, a, B, b, method=7, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), want), (T, a, B, b, e)
+        # element-aligned only
+        raw = torch.zeros(n * e + 64, dtype=torch.uint8, device="cuda")
+        view = raw[e:e + n * e]
+        view.copy_(torch.from_numpy(src.view(np.uint8).copy()).cuda())
+        L.transpose_0100(view, T, a, B, b, method=7, elem_bytes=e)
+        assert np.array_equal(from_dev(view, e), want), (T, a, B, b, e, "un")
+    assert L.lib().lm_device_status(None) == 0
+    # too large for shared memory: refused, buffer unchanged
+    from libmarshal_gb300.lm import LMError
+    n = (48 << 20) // e
+    keep = torch.from_numpy(O.random_bits(n, e, 5).view(np.uint8).copy()).cuda()
+    d = keep.clone()
+    with pytest.raises(LMError):
+        L.transpose_0100(d, 1, 8192, n // 8192, 1, method=7, elem_bytes=e)
+    torch.cuda.synchronize()
+    assert torch.equal(d, keep)
+
+
+def test_resident_form_is_the_route_for_7200x1800(L):
+    """The 7200 x 1800 transposition of bytes and half-words (13 and 26 MB)
+    fits the shared memory of all SMs: the planner runs it as the resident
+    form, one launch."""
+    for e in (1, 2):
+        src = O.random_bits(7200 * 1800, e, 11)
+        d = to_dev(src)
+        L.prof_collect()
+        L.prof_enable(True)
+        try:
+            L.transpose_100(d, 7200, 1800, 1, elem_bytes=e)
+            from_dev(d, e)
+        finally:
+            L.prof_enable(False)
+        ran = L.prof_collect()
+        assert list(ran) == ["resident"], ran
+        assert ran["resident"][0] == 1
+        assert np.array_equal(from_dev(d, e), O.t100(src, 7200, 1800, 1))
