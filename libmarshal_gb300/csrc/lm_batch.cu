@@ -891,6 +891,50 @@ __device__ void gather_issue(const BJob &j, uint32_t q, unsigned char *buf,
   }
 }
 
+// The same row copies as gather_issue, spread over all kStageThreads
+// threads: a warp issues its lanes' bulk copies one after another (about
+// 30 ns each on GB300), so row r of the block goes to lane r / 8 of warp
+// r % 8 and no warp issues more than 32 of a block's 256 rows at most.
+// gather_row_plan: this thread's row (rowoff[] recorded); gather_arrive: a
+// warp's arrival on `bar` (initialised with one arrival per warp) with the
+// bytes of its rows; after a CTA barrier, gather_row_issue starts the copy.
+struct RowCopy {
+  uintptr_t src;   // 16-byte aligned start
+  uint32_t bytes;  // 0: no row for this thread
+  uint32_t dst;    // offset in the stage
+};
+
+__device__ __forceinline__ RowCopy gather_row_plan(const BJob &j, uint32_t q,
+                                                   uint32_t *rowoff) {
+  RowCopy c{0, 0, 0};
+  const GBlock k = gather_decode(j, q);
+  const uint32_t r = (threadIdx.x & 31) * (kStageThreads / 32) + (threadIdx.x >> 5);
+  if (r >= k.si) return c;
+  const uint32_t len = k.sj * j.b * j.e;
+  const uintptr_t src = (uintptr_t)(j.base + ((uint64_t)k.t * j.tile_elems +
+                                              (uint64_t)(k.i0 + r) * j.row_elems +
+                                              (uint64_t)k.j0 * j.b) * j.e);
+  c.src = src & ~(uintptr_t)15;
+  c.bytes = (uint32_t)(((src + len + 15) & ~(uintptr_t)15) - c.src);
+  c.dst = r * j.pitch;
+  rowoff[r] = c.dst + (uint32_t)(src - c.src);
+  return c;
+}
+
+__device__ __forceinline__ void gather_arrive(uint64_t *bar, uint32_t bytes) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+  if ((threadIdx.x & 31) == 0) mbar_arrive_expect_tx(bar, bytes);
+}
+
+__device__ __forceinline__ void gather_row_issue(const RowCopy &c,
+                                                 unsigned char *buf,
+                                                 uint64_t *bar) {
+  if (!c.bytes) return;
+  fence_proxy_async_smem();
+  bulk_g2s(buf + c.dst, (const void *)c.src, c.bytes, bar);
+}
+
 // All threads: output rows j0..j0+sj-1 of the block, each si*b elements
 // long, from the staged rows.
 template <int E>
@@ -1012,8 +1056,8 @@ __global__ void __launch_bounds__(kStageThreads, MB) k_batch_gather(BatchArgs g)
     s_valid[slot] = 1;
   };
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    mbar_init(&bar[0], kStageThreads / 32);
+    mbar_init(&bar[1], kStageThreads / 32);
     fence_mbar_init();
     s_dead = 0;
     fetch(0);
@@ -1021,9 +1065,12 @@ __global__ void __launch_bounds__(kStageThreads, MB) k_batch_gather(BatchArgs g)
   __syncthreads();
   if (!s_valid[0]) return;
   uint32_t cq = s_q[0];
-  if (warp == 0) {
-    copy_job(&s_jobs[0], &jobs[s_job[0]]);
-    gather_issue(jobs[s_job[0]], cq, smem, rowoff[0], &bar[0]);
+  {
+    if (warp == 0) copy_job(&s_jobs[0], &jobs[s_job[0]]);
+    const RowCopy rc = gather_row_plan(jobs[s_job[0]], cq, rowoff[0]);
+    gather_arrive(&bar[0], rc.bytes);
+    __syncthreads();  // every warp's expected bytes before any copy
+    gather_row_issue(rc, smem, &bar[0]);
   }
   uint32_t parity = 0;   // bit st: phase to wait for on bar[st]
   uint32_t pending = 1;  // bit st: loads issued to stage st, not yet seen
@@ -1035,11 +1082,11 @@ __global__ void __launch_bounds__(kStageThreads, MB) k_batch_gather(BatchArgs g)
     const bool more = s_valid[nx] != 0 && !s_dead;
     const uint32_t nj = s_job[nx], nq = s_q[nx];
     if (more) {
-      if (warp == 0) {
-        copy_job(&s_jobs[nx], &jobs[nj]);
-        gather_issue(jobs[nj], nq, smem + (size_t)nx * g.stage_bytes,
-                     rowoff[nx], &bar[nx]);
-      }
+      if (warp == 0) copy_job(&s_jobs[nx], &jobs[nj]);
+      const RowCopy rc = gather_row_plan(jobs[nj], nq, rowoff[nx]);
+      gather_arrive(&bar[nx], rc.bytes);
+      __syncthreads();  // every warp's expected bytes before any copy
+      gather_row_issue(rc, smem + (size_t)nx * g.stage_bytes, &bar[nx]);
       pending |= 1u << nx;
     }
     // wait for block n (bounded; a load that never lands stops this CTA)
@@ -1995,7 +2042,7 @@ struct ResArgs {
 
 __global__ void __launch_bounds__(kStageThreads, 1) k_resident(ResArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar[kResMaxBlocks];
+  __shared__ __align__(8) uint64_t bar;
   __shared__ __align__(16) BJob s_job;
   __shared__ int s_ok;
   const uint32_t warp = threadIdx.x >> 5, nw = kStageThreads / 32;
@@ -2005,25 +2052,36 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_resident(ResArgs g) {
   uint32_t *rowoff =
       reinterpret_cast<uint32_t *>(smem + (size_t)g.nper * g.stage_bytes);
   if (threadIdx.x == 0) {
-    for (uint32_t k = 0; k < nmine; ++k) mbar_init(&bar[k], 1);
+    mbar_init(&bar, nw);
     fence_mbar_init();
     s_ok = 1;
   }
   if (warp == 0) copy_job(&s_job, &g.job);
   __syncthreads();
-  // one warp per block issues its row copies
-  for (uint32_t k = warp; k < nmine; k += nw)
-    gather_issue(s_job, blockIdx.x + k * gridDim.x,
-                 smem + (size_t)k * g.stage_bytes, rowoff + k * s_job.S,
-                 &bar[k]);
+  // every row of every block by its own bulk copy, spread over all warps;
+  // one barrier for all of them
+  RowCopy rc[kResMaxBlocks];
+  uint32_t bytes = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kResMaxBlocks; ++k)
+    if (k < nmine) {
+      rc[k] = gather_row_plan(s_job, blockIdx.x + k * gridDim.x,
+                              rowoff + k * s_job.S);
+      bytes += rc[k].bytes;
+    }
+  gather_arrive(&bar, bytes);
+  __syncthreads();  // every warp's expected bytes before any copy
+#pragma unroll
+  for (uint32_t k = 0; k < kResMaxBlocks; ++k)
+    if (k < nmine)
+      gather_row_issue(rc[k], smem + (size_t)k * g.stage_bytes, &bar);
   bool landed = true;
   const uint64_t t0 = global_timer_ns();
-  for (uint32_t k = 0; k < nmine && landed; ++k)
-    while (!mbar_try_wait(&bar[k], 0))
-      if (global_timer_ns() - t0 > g.timeout_ns) {
-        landed = false;
-        break;
-      }
+  while (!mbar_try_wait(&bar, 0))
+    if (global_timer_ns() - t0 > g.timeout_ns) {
+      landed = false;
+      break;
+    }
   if (!landed) s_ok = 0;
   __syncthreads();
   // grid barrier: every CTA arrives exactly once, then waits (bounded) for
@@ -2059,9 +2117,8 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_resident(ResArgs g) {
   }
   // nothing may still be landing in shared memory when the CTA exits
   const uint64_t t2 = global_timer_ns();
-  for (uint32_t k = 0; k < nmine; ++k)
-    while (!mbar_try_wait(&bar[k], 0) && global_timer_ns() - t2 < g.timeout_ns) {
-    }
+  while (!mbar_try_wait(&bar, 0) && global_timer_ns() - t2 < g.timeout_ns) {
+  }
 }
 
 namespace {
