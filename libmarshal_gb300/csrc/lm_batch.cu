@@ -651,29 +651,48 @@ __device__ __forceinline__ BandPos band_pos(const BJob &j, uint32_t rank) {
   return p;
 }
 
-// Warp 0: bulk copies of my band of every row of `tile`.
-__device__ void band_issue(const BJob &j, uint64_t tile, uint32_t rank,
-                           unsigned char *buf, uint32_t *rowoff, uint64_t *bar) {
-  const uint32_t lane = threadIdx.x & 31;
+// A warp's arrival on a stage barrier that expects one arrival per warp,
+// with the bytes of the warp's bulk copies.
+__device__ __forceinline__ void gather_arrive(uint64_t *bar, uint32_t bytes) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+  if ((threadIdx.x & 31) == 0) mbar_arrive_expect_tx(bar, bytes);
+}
+
+// All threads: bulk copies of my band of every row of `tile`, spread over
+// the warps (a warp issues its lanes' copies one after another): row r by
+// lane (r / nw) % 32 of warp r % nw.  band_plan records rowoff[] and returns
+// this thread's bytes (for the warp's arrival on the stage barrier, which
+// expects one arrival per warp); after a CTA barrier band_issue starts the
+// copies.
+__device__ __forceinline__ uint32_t band_plan(const BJob &j, uint64_t tile,
+                                              uint32_t rank, uint32_t *rowoff) {
+  const uint32_t nw = blockDim.x >> 5, lane = threadIdx.x & 31;
   const BandPos p = band_pos(j, rank);
-  if (p.len == 0) return;
   const uint64_t row_bytes = (uint64_t)j.row_elems * j.e;
   const char *row0 =
       j.base + (tile * j.tile_elems + (uint64_t)p.bc0 * j.b) * j.e;
   uint32_t bytes = 0;
-  for (uint32_t r = lane; r < j.a; r += 32) {
+  for (uint32_t r = (threadIdx.x >> 5) + nw * lane; r < j.a; r += nw * 32) {
     const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
     const uintptr_t a0 = src & ~(uintptr_t)15;
     const uintptr_t a1 = (src + p.len + 15) & ~(uintptr_t)15;
     bytes += (uint32_t)(a1 - a0);
     rowoff[r] = r * j.pitch + (uint32_t)(src - a0);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+  return bytes;
+}
+
+__device__ __forceinline__ void band_issue(const BJob &j, uint64_t tile,
+                                           uint32_t rank, unsigned char *buf,
+                                           uint64_t *bar) {
+  const uint32_t nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+  const BandPos p = band_pos(j, rank);
+  const uint64_t row_bytes = (uint64_t)j.row_elems * j.e;
+  const char *row0 =
+      j.base + (tile * j.tile_elems + (uint64_t)p.bc0 * j.b) * j.e;
   fence_proxy_async_smem();
-  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
-  __syncwarp();
-  for (uint32_t r = lane; r < j.a; r += 32) {
+  for (uint32_t r = (threadIdx.x >> 5) + nw * lane; r < j.a; r += nw * 32) {
     const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
     const uintptr_t a0 = src & ~(uintptr_t)15;
     const uintptr_t a1 = (src + p.len + 15) & ~(uintptr_t)15;
@@ -724,12 +743,13 @@ __device__ void band_store(const BJob &j, uint64_t tile, uint32_t rank,
   }
 }
 
-// Warp 0 is the producer: it waits for the bulk copies of item n, arrives
-// on the cluster barrier with release semantics (its shared-memory writes:
-// job, row offsets, rank 0's claims), then issues the copies of item n+1.
-// The other warps write item n and arrive relaxed: the barrier only has to
-// order every CTA's completed loads of a tile before any CTA's stores to it,
-// and a relaxed arrive does not wait for the earlier global stores to drain.
+// Warp 0 waits for the bulk copies of item n and arrives on the cluster
+// barrier with release semantics (its shared-memory writes: job, tile,
+// rank 0's claims); the other warps arrive relaxed: the barrier only has to
+// order every CTA's completed loads of a tile before any CTA's stores to
+// it, and a relaxed arrive does not wait for the earlier global stores to
+// drain.  After it every warp issues its share of item n+1's row copies,
+// then the other warps write item n.
 __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar[2];
@@ -743,8 +763,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
   const uint32_t warp = threadIdx.x >> 5;
   const bool leader = rank == 0 && threadIdx.x == 0;
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    mbar_init(&bar[0], kBatchThreads / 32);
+    mbar_init(&bar[1], kBatchThreads / 32);
     fence_mbar_init();
     s_ok = 1;
   }
@@ -754,12 +774,22 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
   uint32_t cur = item0[0];
   if (leader) s_item[1] = atomicAdd(g.counter, 1u);  // read after the next sync
   uint32_t parity = 0, pending = 0;
-  if (cur < g.nitems && warp == 0) {
-    const BItem it = g.items[cur];
-    copy_job(&s_jobs[0], &g.jobs[it.job]);
-    if ((threadIdx.x & 31) == 0) s_tile[0] = it.tile0;
-    band_issue(g.jobs[it.job], it.tile0, rank, smem, rowoff[0], &bar[0]);
-  }
+  // stages the band of item k's tile into stage st (every thread)
+  auto stage_item = [&](uint32_t k, int st) {
+    const BItem it = g.items[k];
+    const BJob &j = g.jobs[it.job];
+    const bool has = band_pos(j, rank).len > 0;
+    if (has) gather_arrive(&bar[st], band_plan(j, it.tile0, rank, rowoff[st]));
+    __syncthreads();  // every warp's expected bytes before any copy
+    if (has)
+      band_issue(j, it.tile0, rank, smem + (size_t)st * g.stage_bytes,
+                 &bar[st]);
+    if (warp == 0) {
+      copy_job(&s_jobs[st], &j);
+      if ((threadIdx.x & 31) == 0) s_tile[st] = it.tile0;
+    }
+  };
+  if (cur < g.nitems) stage_item(cur, 0);
   for (uint32_t n = 0; cur < g.nitems; ++n) {
     const int st = n & 1, nx = st ^ 1;
     if (warp == 0) {
@@ -788,16 +818,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch_band(BatchArgs g) {
     }
     cluster_wait_acquire();  // every band of item n staged; claim n+1 visible
     const uint32_t nxt = item0[nx];
+    if (nxt < g.nitems && s_ok) stage_item(nxt, nx);
     if (warp == 0) {
-      if (nxt < g.nitems) {
-        const BItem in = g.items[nxt];
-        copy_job(&s_jobs[nx], &g.jobs[in.job]);
-        if ((threadIdx.x & 31) == 0) s_tile[nx] = in.tile0;
-        __syncwarp();
-        if (s_ok)
-          band_issue(g.jobs[in.job], in.tile0, rank,
-                     smem + (size_t)nx * g.stage_bytes, rowoff[nx], &bar[nx]);
-      }
       if (leader) s_item[st] = atomicAdd(g.counter, 1u);  // claim n+2
     } else if (s_ok) {
       const BJob &j = s_jobs[st];
@@ -919,12 +941,6 @@ __device__ __forceinline__ RowCopy gather_row_plan(const BJob &j, uint32_t q,
   c.dst = r * j.pitch;
   rowoff[r] = c.dst + (uint32_t)(src - c.src);
   return c;
-}
-
-__device__ __forceinline__ void gather_arrive(uint64_t *bar, uint32_t bytes) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
-  if ((threadIdx.x & 31) == 0) mbar_arrive_expect_tx(bar, bytes);
 }
 
 __device__ __forceinline__ void gather_row_issue(const RowCopy &c,

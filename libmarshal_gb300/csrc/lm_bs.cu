@@ -157,8 +157,9 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100_band(BsArgs g) {
   const uint32_t band_elems = nbu * g.b;
   const uint32_t len = band_elems * E;          // bytes per row segment
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t nw = kBsThreads / 32;
   if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(&bar, nw);  // one arrival per warp
     fence_mbar_init();
     s_ok = 1;
   }
@@ -168,10 +169,13 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100_band(BsArgs g) {
     const uint64_t e0 = tile * (uint64_t)g.tile_elems;
     T *t = reinterpret_cast<T *>(g.base) + e0;
     // ---- load: one bulk copy per row (16-byte aligned superset of the band
-    // segment; rowoff[] records where the segment starts in shared memory)
-    if (warp == 0 && len > 0) {
+    // segment; rowoff[] records where the segment starts in shared memory),
+    // spread over the warps (a warp issues its lanes' copies one after
+    // another): row r by lane (r / nw) % 32 of warp r % nw.  Each warp
+    // arrives with its bytes; a CTA barrier; then the copies.
+    if (len > 0) {
       uint32_t bytes = 0;
-      for (uint32_t r = lane; r < g.a; r += 32) {
+      for (uint32_t r = warp + nw * lane; r < g.a; r += nw * 32) {
         const char *src = reinterpret_cast<const char *>(
             t + (uint64_t)r * g.row_elems + (uint64_t)bc0 * g.b);
         const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
@@ -181,10 +185,10 @@ __global__ void __launch_bounds__(kBsThreads) k_bs0100_band(BsArgs g) {
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
-      fence_proxy_async_smem();
       if (lane == 0) mbar_arrive_expect_tx(&bar, bytes);
-      __syncwarp();
-      for (uint32_t r = lane; r < g.a; r += 32) {
+      __syncthreads();  // every warp's expected bytes before any copy
+      fence_proxy_async_smem();
+      for (uint32_t r = warp + nw * lane; r < g.a; r += nw * 32) {
         const char *src = reinterpret_cast<const char *>(
             t + (uint64_t)r * g.row_elems + (uint64_t)bc0 * g.b);
         const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;

@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
   };
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full[s], g.tma ? 1u : kProducerWarps * 32u);
+      mbar_init(&full[s], g.tma ? (uint32_t)kProducerWarps : kProducerWarps * 32u);
       mbar_init(&ready[s], 1);
       // freed by every writer warp and by the publisher, so a stage is not
       // refilled (its `full` barrier not completed again) before the
@@ -326,30 +326,16 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
     const uint32_t pt = threadIdx.x;  // 0 .. 127
     constexpr uint32_t kP = kProducerWarps * 32;
     uint32_t issued = 0;
-    // this lane's rows t = lane + 32m: first stashed group and stash offset
-    uint64_t rJi[kMaxRowBlocks], rro[kMaxRowBlocks];
-#pragma unroll
-    for (int m = 0; m < kMaxRowBlocks; ++m) {
-      const uint32_t t = lane + 32 * m;
-      rJi[m] = t < Wc ? first_group(i0 + t, g) : ~0ull;
-      rro[m] = t < Wc ? g.roff[i0 + t] : 0;
-    }
+    // with bulk copies each producer thread owns one row of the chunk (a
+    // warp issues its lanes' copies one after another, so the rows are
+    // spread over the four warps): row t = 4 * lane + warp, its first
+    // stashed group and stash offset
+    const uint32_t my_t = lane * kProducerWarps + warp;
+    const bool my_row = g.tma && my_t < Wc;
+    const uint64_t my_Ji = my_row ? first_group(i0 + my_t, g) : ~0ull;
+    const uint64_t my_ro = my_row ? g.roff[i0 + my_t] : 0;
     for (uint32_t J = 0; J < g.G; ++J) {
       const uint32_t s = J % kStages;
-      bool stop = !s_ok;
-      if (!stop && J >= kStages)
-        stop = !wait_bar(&empty[s], ((J / kStages) - 1) & 1);
-      // the four producer warps take the same decision: s_pstop is written
-      // only before the first barrier and read only between the two
-      if (stop) s_pstop = 1;
-      asm volatile("bar.sync 1, %0;" ::"n"(kP) : "memory");
-      const bool stop_all = s_pstop != 0;
-      asm volatile("bar.sync 1, %0;" ::"n"(kP) : "memory");
-      if (stop_all) {
-        s_ok = 0;
-        break;
-      }
-      issued = J + 1;
       const uint64_t col0 = (uint64_t)J * g.g;
       const uint32_t len = (uint32_t)min64(g.g, g.B - col0) * U;
       unsigned char *sb = stage(s);
@@ -358,37 +344,44 @@ __global__ void __launch_bounds__(kWaveThreads, 2) k_stash_wave(StashArgs g) {
         return J >= Ji ? g.stash + ro + (col0 - Ji * g.g) * U
                        : g.base + (i * g.B + col0) * U;
       };
+      bool stop = !s_ok;
+      if (!stop && J >= kStages)
+        stop = !wait_bar(&empty[s], ((J / kStages) - 1) & 1);
+      // the four producer warps take the same decision: s_pstop is written
+      // only before the first barrier and read only between the two
+      if (stop) s_pstop = 1;
+      asm volatile("bar.sync 1, %0;" ::"n"(kP) : "memory");
+      const bool stop_all = s_pstop != 0;
+      // bulk copies: every producer warp arrives on the stage with the
+      // bytes of its rows before the second barrier, so all expected bytes
+      // are counted before any copy starts
+      uintptr_t my_a0 = 0;
+      uint32_t my_bytes = 0;
+      if (g.tma && !stop_all) {
+        if (my_row) {
+          const char *src = strip(i0 + my_t, my_Ji, my_ro);
+          my_a0 = (uintptr_t)src & ~(uintptr_t)15;
+          my_bytes = (uint32_t)((((uintptr_t)src + len + 15) & ~(uintptr_t)15) - my_a0);
+          rowoff(s)[my_t] = my_t * g.pitch + (uint32_t)((uintptr_t)src - my_a0);
+        }
+        uint32_t bytes = my_bytes;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          bytes += __shfl_xor_sync(kFull, bytes, o);
+        if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kP) : "memory");
+      if (stop_all) {
+        s_ok = 0;
+        break;
+      }
+      issued = J + 1;
       if (g.tma) {
-        // warp 0: one bulk copy per row (16-byte aligned superset)
-        if (warp == 0) {
-          uint32_t bytes = 0;
-#pragma unroll
-          for (int m = 0; m < kMaxRowBlocks; ++m) {
-            const uint32_t t = lane + 32 * m;
-            if (t >= Wc) continue;
-            const char *src = strip(i0 + t, rJi[m], rro[m]);
-            const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
-            const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
-            bytes += (uint32_t)(a1 - a0);
-            rowoff(s)[t] = t * g.pitch + (uint32_t)((uintptr_t)src - a0);
-          }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1)
-            bytes += __shfl_xor_sync(kFull, bytes, o);
+        // one bulk copy per row (16-byte aligned superset)
+        if (my_bytes) {
           fence_proxy_async_smem();
-          __syncwarp();
-          if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes);
-          __syncwarp();
-#pragma unroll
-          for (int m = 0; m < kMaxRowBlocks; ++m) {
-            const uint32_t t = lane + 32 * m;
-            if (t >= Wc) continue;
-            const char *src = strip(i0 + t, rJi[m], rro[m]);
-            const uintptr_t a0 = (uintptr_t)src & ~(uintptr_t)15;
-            const uintptr_t a1 = ((uintptr_t)src + len + 15) & ~(uintptr_t)15;
-            bulk_g2s(sb + (size_t)t * g.pitch, (const void *)a0,
-                     (uint32_t)(a1 - a0), &full[s]);
-          }
+          bulk_g2s(sb + (size_t)my_t * g.pitch, (const void *)my_a0, my_bytes,
+                   &full[s]);
         }
       } else {
         // 16-byte chunks per row (upper bound; chunks past the strip skipped)
