@@ -563,14 +563,18 @@ __device__ __forceinline__ void store_b1(const unsigned char *buf,
   }
 }
 
-// store_b1 for 1- and 2-byte elements with whole 16-byte output vectors:
-// lane l of a warp takes 32-bit word column w (4/E staged columns) of a
-// group of 16/E staged rows (one word per row: the warp reads 32
-// consecutive words of a row at a time, no bank conflicts), transposes the
-// bytes in registers and writes one 16-byte vector to each of its 4/E
-// output rows.  Staged rows must start on 32-bit words, nrows be a multiple
-// of 16/E, ncols of 4/E, and the vectors dst + jj*ostride + i land on 16
-// bytes (ostride*E and the block's first row a multiple of 16 bytes).
+// store_b1 for 1- and 2-byte elements with whole 16-byte output vectors.
+// A group is 16/E staged rows (one output vector per staged column); lane
+// l of a warp takes group 8c + l % 8 and 32-bit word column 4d + l / 8 (4/E
+// staged columns), reads the group's 16/E words of that column, transposes
+// the bytes in registers and writes one 16-byte vector to each of its 4/E
+// output rows: the eight lanes of a word column write eight consecutive
+// vectors (128 bytes) of the same output row.  The stage shifts the rows of
+// group g by 16 g bytes so the eight groups read at once sit in distinct
+// bank groups.  Staged rows must start on 32-bit words,
+// nrows be a multiple of 16/E, ncols of 4/E, and the vectors dst +
+// jj*ostride + i land on 16 bytes (ostride*E and the block's first row a
+// multiple of 16 bytes).
 template <int E>
 __device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
                                              const uint32_t *rowoff,
@@ -583,10 +587,11 @@ __device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
   constexpr uint32_t CW = 4 / E;   // staged columns per 32-bit word
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t ngr = nrows / RW, nwc = ncols / CW;
-  const uint32_t nch = (nwc + 31) / 32;
-  for (uint32_t u = warp; u < ngr * nch; u += nwarps) {
-    const uint32_t g = u / nch, wc = (u - g * nch) * 32 + lane;
-    if (wc >= nwc) continue;
+  const uint32_t ngc = (ngr + 7) / 8, nwd = (nwc + 3) / 4;
+  for (uint32_t u = warp; u < ngc * nwd; u += nwarps) {
+    const uint32_t d = u / ngc, gc = u - d * ngc;
+    const uint32_t g = gc * 8 + (lane & 7), wc = d * 4 + (lane >> 3);
+    if (g >= ngr || wc >= nwc) continue;
     const unsigned char *col = buf + wc * 4;
     const uint32_t r0 = g * RW;
     auto word = [&](uint32_t k) {
@@ -880,41 +885,8 @@ __device__ __forceinline__ GBlock gather_decode(const BJob &j, uint32_t q) {
   return k;
 }
 
-// Warp 0: one bulk copy per row of the block (the 16-byte aligned superset
-// of its row segment) into `buf`; rowoff[] records where each segment starts.
-__device__ void gather_issue(const BJob &j, uint32_t q, unsigned char *buf,
-                             uint32_t *rowoff, uint64_t *bar) {
-  const uint32_t lane = threadIdx.x & 31;
-  const GBlock k = gather_decode(j, q);
-  const uint32_t len = k.sj * j.b * j.e;
-  const uint64_t row_bytes = (uint64_t)j.row_elems * j.e;
-  const char *row0 = j.base + ((uint64_t)k.t * j.tile_elems +
-                               (uint64_t)k.i0 * j.row_elems +
-                               (uint64_t)k.j0 * j.b) * j.e;
-  uint32_t bytes = 0;
-  for (uint32_t r = lane; r < k.si; r += 32) {
-    const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
-    const uintptr_t a0 = src & ~(uintptr_t)15;
-    const uintptr_t a1 = (src + len + 15) & ~(uintptr_t)15;
-    bytes += (uint32_t)(a1 - a0);
-    rowoff[r] = r * j.pitch + (uint32_t)(src - a0);
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
-  fence_proxy_async_smem();
-  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
-  __syncwarp();
-  for (uint32_t r = lane; r < k.si; r += 32) {
-    const uintptr_t src = (uintptr_t)(row0 + r * row_bytes);
-    const uintptr_t a0 = src & ~(uintptr_t)15;
-    const uintptr_t a1 = (src + len + 15) & ~(uintptr_t)15;
-    bulk_g2s(buf + (size_t)r * j.pitch, (const void *)a0, (uint32_t)(a1 - a0),
-             bar);
-  }
-}
-
-// The same row copies as gather_issue, spread over all kStageThreads
-// threads: a warp issues its lanes' bulk copies one after another (about
+// One bulk copy per row of the block (the 16-byte aligned superset of its
+// row segment), spread over all kStageThreads threads: a warp issues its lanes' bulk copies one after another (about
 // 30 ns each on GB300), so row r of the block goes to lane r / 8 of warp
 // r % 8 and no warp issues more than 32 of a block's 256 rows at most.
 // gather_row_plan: this thread's row (rowoff[] recorded); gather_arrive: a
@@ -938,7 +910,10 @@ __device__ __forceinline__ RowCopy gather_row_plan(const BJob &j, uint32_t q,
                                               (uint64_t)k.j0 * j.b) * j.e);
   c.src = src & ~(uintptr_t)15;
   c.bytes = (uint32_t)(((src + len + 15) & ~(uintptr_t)15) - c.src);
-  c.dst = r * j.pitch;
+  // vectorized narrow store: the rows of group r*e/16 shifted by 16 bytes
+  // per group (the shifts only grow, so rows never overlap), so the eight
+  // consecutive groups a warp reads at once fall in distinct bank groups
+  c.dst = r * j.pitch + (j.vb1 ? 16 * (r * j.e / 16) : 0);
   rowoff[r] = c.dst + (uint32_t)(src - c.src);
   return c;
 }
@@ -1600,7 +1575,10 @@ static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.div_nIJ = make_fastdiv(j.nIJ);
   j.bytes = nz.T * nz.a * nz.B * nz.b * (uint64_t)nz.e;
   *nblk = nz.T * nI * nJ;
-  *stage_bytes = ((size_t)S * sp + 127) / 128 * 128;
+  // (rows shifted by 16 bytes per group of 16/e rows for the vectorized
+  // narrow store)
+  *stage_bytes =
+      ((size_t)S * sp + (j.vb1 ? 16 * ((S * nz.e + 15) / 16) : 0) + 127) / 128 * 128;
   return true;
 }
 
