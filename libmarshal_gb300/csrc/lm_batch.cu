@@ -83,8 +83,11 @@ struct BJob {
   uint32_t tpitch, kt;
   FastDiv div_nc, div_rows;
   // staged form, b == 1 and 1- or 2-byte elements: staged rows start on
-  // 32-bit words and output vectors on 16 bytes (store_b1_vec applies)
-  uint32_t vb1;
+  // 32-bit words and output vectors on 16 bytes (store_b1_vec applies);
+  // else vbc = the widest output vector (16, 8 or 4 bytes) the output rows
+  // allow (store_b1_vecc), 0 for none; vrw = staged rows per output vector
+  // of either store (their groups are shifted in the stage), 0 for none
+  uint32_t vb1, vbc, vrw;
 };
 
 struct BItem {
@@ -635,6 +638,60 @@ __device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
   }
 }
 
+// store_b1 with whole VB-byte output vectors for staged rows that need not
+// start on 32-bit words: lane l of a warp takes group 8c + l % 8 of VB/E
+// staged rows and staged column 4d + l / 8, gathers the group's VB/E
+// elements of that column one by one and writes them as one vector, so the
+// eight lanes of a column write eight consecutive vectors of one output
+// row.  Groups are shifted in the stage as for store_b1_vec.  nrows must be
+// a multiple of VB/E and the vectors dst + jj*ostride + i land on VB bytes.
+template <int E, int VB>
+__device__ __forceinline__ void store_b1_vecc(const unsigned char *buf,
+                                              const uint32_t *rowoff,
+                                              uint32_t nrows, uint32_t ncols,
+                                              typename Elem<E>::T *dst,
+                                              uint32_t ostride, uint32_t warp,
+                                              uint32_t nwarps) {
+  static_assert(E == 1 || E == 2, "narrow elements only");
+  static_assert(VB == 4 || VB == 8 || VB == 16, "4-, 8- or 16-byte vectors");
+  constexpr uint32_t RW = VB / E;  // staged rows per output vector
+  constexpr uint32_t NW = VB / 4;  // 32-bit words per vector
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t ngr = nrows / RW;
+  const uint32_t ngc = (ngr + 7) / 8, nd = (ncols + 3) / 4;
+  for (uint32_t u = warp; u < ngc * nd; u += nwarps) {
+    const uint32_t d = u / ngc, gc = u - d * ngc;
+    const uint32_t g = gc * 8 + (lane & 7), jj = d * 4 + (lane >> 3);
+    if (g >= ngr || jj >= ncols) continue;
+    const uint32_t r0 = g * RW;
+    const unsigned char *col = buf + jj * E;
+    uint32_t w[NW];
+#pragma unroll
+    for (uint32_t q = 0; q < NW; ++q) {
+      if constexpr (E == 1) {
+        const uint32_t b0 = col[rowoff[r0 + 4 * q]];
+        const uint32_t b1 = col[rowoff[r0 + 4 * q + 1]];
+        const uint32_t b2 = col[rowoff[r0 + 4 * q + 2]];
+        const uint32_t b3 = col[rowoff[r0 + 4 * q + 3]];
+        w[q] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+      } else {
+        const uint32_t h0 =
+            *reinterpret_cast<const unsigned short *>(col + rowoff[r0 + 2 * q]);
+        const uint32_t h1 = *reinterpret_cast<const unsigned short *>(
+            col + rowoff[r0 + 2 * q + 1]);
+        w[q] = h0 | (h1 << 16);
+      }
+    }
+    typename Elem<E>::T *p = dst + (uint64_t)jj * ostride + r0;
+    if constexpr (VB == 16)
+      __stcg(reinterpret_cast<uint4 *>(p), make_uint4(w[0], w[1], w[2], w[3]));
+    else if constexpr (VB == 8)
+      __stcg(reinterpret_cast<uint2 *>(p), make_uint2(w[0], w[1]));
+    else
+      __stcg(reinterpret_cast<unsigned int *>(p), w[0]);
+  }
+}
+
 // Tiles larger than one CTA's shared memory, processed by persistent
 // clusters: rank 0 claims items and shares them through distributed shared
 // memory; each CTA stages a column band of the tile with bulk copies
@@ -910,10 +967,10 @@ __device__ __forceinline__ RowCopy gather_row_plan(const BJob &j, uint32_t q,
                                               (uint64_t)k.j0 * j.b) * j.e);
   c.src = src & ~(uintptr_t)15;
   c.bytes = (uint32_t)(((src + len + 15) & ~(uintptr_t)15) - c.src);
-  // vectorized narrow store: the rows of group r*e/16 shifted by 16 bytes
+  // vectorized narrow stores: the rows of group r / vrw shifted by 16 bytes
   // per group (the shifts only grow, so rows never overlap), so the eight
   // consecutive groups a warp reads at once fall in distinct bank groups
-  c.dst = r * j.pitch + (j.vb1 ? 16 * (r * j.e / 16) : 0);
+  c.dst = r * j.pitch + (j.vrw ? 16 * (r / j.vrw) : 0);
   rowoff[r] = c.dst + (uint32_t)(src - c.src);
   return c;
 }
@@ -964,6 +1021,16 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
       if (j.vb1 && k.si % (16 / E) == 0 && k.sj % (4 / E) == 0) {
         store_b1_vec<E>(buf, rowoff, k.si, k.sj, dst, j.a, threadIdx.x >> 5,
                         kStageThreads / 32);
+        return;
+      }
+      if (j.vbc && k.si % (j.vbc / E) == 0) {
+        const uint32_t w = threadIdx.x >> 5, nw = kStageThreads / 32;
+        if (j.vbc == 16)
+          store_b1_vecc<E, 16>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw);
+        else if (j.vbc == 8)
+          store_b1_vecc<E, 8>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw);
+        else
+          store_b1_vecc<E, 4>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw);
         return;
       }
     }
@@ -1565,6 +1632,15 @@ static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
            (nz.B * nz.e) % 4 == 0 && (Sj * nz.e) % 4 == 0 &&
            (nz.a * nz.e) % 16 == 0 && (S * nz.e) % 16 == 0)
               ? 1u : 0u;
+  j.vbc = 0;
+  if (!j.vb1 && nz.b == 1 && nz.e <= 2)
+    for (uint32_t w : {16u, 8u, 4u})
+      if ((uintptr_t)jb.buf % w == 0 && (nz.a * nz.e) % w == 0 &&
+          (S * nz.e) % w == 0) {
+        j.vbc = w;
+        break;
+      }
+  j.vrw = j.vb1 ? 16 / nz.e : j.vbc / nz.e;
   j.div_nv16 = make_fastdiv(j.nv16 ? j.nv16 : 1);
   j.ng8 = (S + 7) / 8;
   j.div_ng8 = make_fastdiv(j.ng8);
@@ -1575,10 +1651,11 @@ static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
   j.div_nIJ = make_fastdiv(j.nIJ);
   j.bytes = nz.T * nz.a * nz.B * nz.b * (uint64_t)nz.e;
   *nblk = nz.T * nI * nJ;
-  // (rows shifted by 16 bytes per group of 16/e rows for the vectorized
-  // narrow store)
+  // (rows shifted by 16 bytes per group of vrw rows for the vectorized
+  // narrow stores)
   *stage_bytes =
-      ((size_t)S * sp + (j.vb1 ? 16 * ((S * nz.e + 15) / 16) : 0) + 127) / 128 * 128;
+      ((size_t)S * sp + (j.vrw ? 16 * ((S + j.vrw - 1) / j.vrw) : 0) + 127) /
+      128 * 128;
   return true;
 }
 

@@ -573,12 +573,15 @@ def test_full_transpose_reference_suite(L):
 def test_staged_narrow_vector_store(L, e):
     """The staged form (method 6) on 1- and 2-byte one-element units: shapes
     whose staged rows start on 32-bit words and whose output vectors land on
-    16 bytes take the vectorized transposed store (whole 16-byte output
-    vectors), the others the element-wise one; several tiles, ragged block
-    edges; bit-exact against the oracle."""
+    16 bytes take the word-column vector store, shapes whose output rows
+    allow 16-, 8- or 4-byte vectors the element-column vector store (rows
+    on any boundary), the others the element-wise one; several tiles,
+    ragged block edges; bit-exact against the oracle."""
     shapes = [(1, 7200, 1800), (1, 1024, 4000), (3, 256, 1000),
               (1, 4096, 500), (2, 48, 2000), (1, 7200, 1801),
-              (1, 1000, 1000), (1, 336, 4004), (4, 160, 24)]
+              (1, 1000, 1000), (1, 336, 4004), (4, 160, 24),
+              (1, 500, 1003), (2, 52, 777), (1, 4100, 999), (1, 500, 1001),
+              (3, 6, 1000), (1, 4098, 333), (5, 1000, 37)]
     for (T, a, B) in shapes:
         src = O.random_bits(T * a * B, e, T + a + B)
         d = to_dev(src)
