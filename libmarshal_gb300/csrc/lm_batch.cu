@@ -84,8 +84,8 @@ struct BJob {
   FastDiv div_nc, div_rows;
   // staged form, b == 1 and 1- or 2-byte elements: staged rows start on
   // 32-bit words and output vectors on 16 bytes (store_b1_vec applies);
-  // else vbc = the widest output vector (16, 8 or 4 bytes) the output rows
-  // allow (store_b1_vecc), 0 for none; vrw = staged rows per output vector
+  // else vbc = the widest output vector (16, 8 or 4 bytes; 16 for 4- and
+  // 8-byte elements) the output rows allow (store_b1_vecc), 0 for none; vrw = staged rows per output vector
   // of either store (their groups are shifted in the stage), 0 for none
   uint32_t vb1, vbc, vrw;
 };
@@ -578,13 +578,19 @@ __device__ __forceinline__ void store_b1(const unsigned char *buf,
 // nrows be a multiple of 16/E, ncols of 4/E, and the vectors dst +
 // jj*ostride + i land on 16 bytes (ostride*E and the block's first row a
 // multiple of 16 bytes).
+// Row r0 + k of a group starts at rowoff[r0] rounded down to 16 bytes,
+// plus k pitches, plus the row's own offset within 16 bytes (which advances
+// by rb = the global row length mod 16 from row to row): one table read per
+// group instead of one per row (the eight groups' table entries share
+// banks).
 template <int E>
 __device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
                                              const uint32_t *rowoff,
                                              uint32_t nrows, uint32_t ncols,
                                              typename Elem<E>::T *dst,
                                              uint32_t ostride, uint32_t warp,
-                                             uint32_t nwarps) {
+                                             uint32_t nwarps, uint32_t pitch,
+                                             uint32_t rb) {
   static_assert(E == 1 || E == 2, "narrow elements only");
   constexpr uint32_t RW = 16 / E;  // staged rows per output vector
   constexpr uint32_t CW = 4 / E;   // staged columns per 32-bit word
@@ -595,10 +601,12 @@ __device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
     const uint32_t d = u / ngc, gc = u - d * ngc;
     const uint32_t g = gc * 8 + (lane & 7), wc = d * 4 + (lane >> 3);
     if (g >= ngr || wc >= nwc) continue;
-    const unsigned char *col = buf + wc * 4;
     const uint32_t r0 = g * RW;
+    const uint32_t o0 = rowoff[r0], m0 = o0 & 15;
+    const unsigned char *col = buf + wc * 4 + (o0 - m0);
     auto word = [&](uint32_t k) {
-      return *reinterpret_cast<const uint32_t *>(col + rowoff[r0 + k]);
+      return *reinterpret_cast<const uint32_t *>(col + k * pitch +
+                                                 ((m0 + k * rb) & 15));
     };
     uint4 out[CW];
 #pragma unroll
@@ -639,7 +647,8 @@ __device__ __forceinline__ void store_b1_vec(const unsigned char *buf,
 }
 
 // store_b1 with whole VB-byte output vectors for staged rows that need not
-// start on 32-bit words: lane l of a warp takes group 8c + l % 8 of VB/E
+// start on 32-bit words (and for 4- and 8-byte elements, with 16-byte
+// vectors of 4 or 2 rows): lane l of a warp takes group 8c + l % 8 of VB/E
 // staged rows and staged column 4d + l / 8, gathers the group's VB/E
 // elements of that column one by one and writes them as one vector, so the
 // eight lanes of a column write eight consecutive vectors of one output
@@ -651,9 +660,10 @@ __device__ __forceinline__ void store_b1_vecc(const unsigned char *buf,
                                               uint32_t nrows, uint32_t ncols,
                                               typename Elem<E>::T *dst,
                                               uint32_t ostride, uint32_t warp,
-                                              uint32_t nwarps) {
-  static_assert(E == 1 || E == 2, "narrow elements only");
+                                              uint32_t nwarps, uint32_t pitch,
+                                              uint32_t rb) {
   static_assert(VB == 4 || VB == 8 || VB == 16, "4-, 8- or 16-byte vectors");
+  static_assert(VB >= E, "a vector holds whole elements");
   constexpr uint32_t RW = VB / E;  // staged rows per output vector
   constexpr uint32_t NW = VB / 4;  // 32-bit words per vector
   const uint32_t lane = threadIdx.x & 31;
@@ -664,22 +674,34 @@ __device__ __forceinline__ void store_b1_vecc(const unsigned char *buf,
     const uint32_t g = gc * 8 + (lane & 7), jj = d * 4 + (lane >> 3);
     if (g >= ngr || jj >= ncols) continue;
     const uint32_t r0 = g * RW;
+    const uint32_t o0 = rowoff[r0], m0 = o0 & 15;
     const unsigned char *col = buf + jj * E;
+    // groups of 8 rows and more: offsets from the group's first row (the
+    // eight groups' table entries would share banks); shorter groups read
+    // the table (their entries fall in distinct banks)
+    auto at = [&](uint32_t k) {
+      if constexpr (RW >= 8)
+        return col + (o0 - m0) + k * pitch + ((m0 + k * rb) & 15);
+      else
+        return col + rowoff[r0 + k];
+    };
     uint32_t w[NW];
 #pragma unroll
     for (uint32_t q = 0; q < NW; ++q) {
       if constexpr (E == 1) {
-        const uint32_t b0 = col[rowoff[r0 + 4 * q]];
-        const uint32_t b1 = col[rowoff[r0 + 4 * q + 1]];
-        const uint32_t b2 = col[rowoff[r0 + 4 * q + 2]];
-        const uint32_t b3 = col[rowoff[r0 + 4 * q + 3]];
+        const uint32_t b0 = *at(4 * q), b1 = *at(4 * q + 1);
+        const uint32_t b2 = *at(4 * q + 2), b3 = *at(4 * q + 3);
         w[q] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
-      } else {
-        const uint32_t h0 =
-            *reinterpret_cast<const unsigned short *>(col + rowoff[r0 + 2 * q]);
-        const uint32_t h1 = *reinterpret_cast<const unsigned short *>(
-            col + rowoff[r0 + 2 * q + 1]);
+      } else if constexpr (E == 2) {
+        const uint32_t h0 = *reinterpret_cast<const unsigned short *>(at(2 * q));
+        const uint32_t h1 =
+            *reinterpret_cast<const unsigned short *>(at(2 * q + 1));
         w[q] = h0 | (h1 << 16);
+      } else if constexpr (E == 4) {
+        w[q] = *reinterpret_cast<const uint32_t *>(at(q));
+      } else {
+        // 8-byte elements: word q is half q % 2 of row q / 2
+        w[q] = reinterpret_cast<const uint32_t *>(at(q / 2))[q % 2];
       }
     }
     typename Elem<E>::T *p = dst + (uint64_t)jj * ostride + r0;
@@ -1017,22 +1039,27 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
     return;
   }
   if (j.b == 1) {
+    const uint32_t w = threadIdx.x >> 5, nw = kStageThreads / 32;
+    const uint32_t rb = (j.row_elems * E) & 15;  // row length mod 16
     if constexpr (E <= 2) {
       if (j.vb1 && k.si % (16 / E) == 0 && k.sj % (4 / E) == 0) {
-        store_b1_vec<E>(buf, rowoff, k.si, k.sj, dst, j.a, threadIdx.x >> 5,
-                        kStageThreads / 32);
+        store_b1_vec<E>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw, j.pitch, rb);
         return;
       }
-      if (j.vbc && k.si % (j.vbc / E) == 0) {
-        const uint32_t w = threadIdx.x >> 5, nw = kStageThreads / 32;
-        if (j.vbc == 16)
-          store_b1_vecc<E, 16>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw);
-        else if (j.vbc == 8)
-          store_b1_vecc<E, 8>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw);
+    }
+    if (j.vbc && k.si % (j.vbc / E) == 0) {
+      if (j.vbc == 16)
+        store_b1_vecc<E, 16>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw, j.pitch,
+                             rb);
+      else if constexpr (E <= 2) {
+        if (j.vbc == 8)
+          store_b1_vecc<E, 8>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw,
+                              j.pitch, rb);
         else
-          store_b1_vecc<E, 4>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw);
-        return;
+          store_b1_vecc<E, 4>(buf, rowoff, k.si, k.sj, dst, j.a, w, nw,
+                              j.pitch, rb);
       }
+      return;
     }
     store_b1<E>(buf, rowoff, k.si, k.sj, j.ng8, j.div_ng8, dst, j.a,
                 threadIdx.x >> 5, kStageThreads / 32);
@@ -1633,9 +1660,10 @@ static bool staged_job(BJob &j, const lm_job &jb, const Normalized &nz,
            (nz.a * nz.e) % 16 == 0 && (S * nz.e) % 16 == 0)
               ? 1u : 0u;
   j.vbc = 0;
-  if (!j.vb1 && nz.b == 1 && nz.e <= 2)
+  if (!j.vb1 && nz.b == 1)
     for (uint32_t w : {16u, 8u, 4u})
-      if ((uintptr_t)jb.buf % w == 0 && (nz.a * nz.e) % w == 0 &&
+      if (w >= (uint32_t)nz.e && (w == 16 || nz.e <= 2) &&
+          (uintptr_t)jb.buf % w == 0 && (nz.a * nz.e) % w == 0 &&
           (S * nz.e) % w == 0) {
         j.vbc = w;
         break;

@@ -569,14 +569,15 @@ def test_full_transpose_reference_suite(L):
     assert L.lib().lm_device_status(None) == 0
 
 
-@pytest.mark.parametrize("e", [1, 2])
+@pytest.mark.parametrize("e", [1, 2, 4, 8])
 def test_staged_narrow_vector_store(L, e):
-    """The staged form (method 6) on 1- and 2-byte one-element units: shapes
+    """The staged form (method 6) on one-element units: 1- and 2-byte shapes
     whose staged rows start on 32-bit words and whose output vectors land on
     16 bytes take the word-column vector store, shapes whose output rows
-    allow 16-, 8- or 4-byte vectors the element-column vector store (rows
-    on any boundary), the others the element-wise one; several tiles,
-    ragged block edges; bit-exact against the oracle."""
+    allow 16-, 8- or 4-byte vectors (16 for 4- and 8-byte elements) the
+    element-column vector store (rows on any boundary), the others the
+    element-wise one; several tiles, ragged block edges; bit-exact against
+    the oracle."""
     shapes = [(1, 7200, 1800), (1, 1024, 4000), (3, 256, 1000),
               (1, 4096, 500), (2, 48, 2000), (1, 7200, 1801),
               (1, 1000, 1000), (1, 336, 4004), (4, 160, 24),
