@@ -202,6 +202,15 @@ bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
                         int x_size, int y_size, int pad_size, int unpad,
                         long long stall_block, unsigned long long timeout_ns);
 
+/* Failure-detection hook (no reference counterpart): the shared-memory
+ * resident form of 0100(A, a, B, b) (lm_transpose_0100_method, method 7)
+ * with its grid barrier waiting for one arrival more than there are CTAs.
+ * Every CTA gives up after timeout_ns without writing; the call must return
+ * true, leave the buffer unchanged and the CUDA context usable. */
+bool lm_debug_resident_stall(lm_stream_t stream, void *buf, int elem_bytes,
+                             int A, int a, int B, int b,
+                             unsigned long long timeout_ns);
+
 /* ---- batched conversion (no reference counterpart) -------------------------
  * A batch is a list of independent in-place jobs, each on its own device
  * buffer (buffers must not overlap), of any op and element width.

@@ -974,6 +974,31 @@ bool lm_debug_pad_stall(lm_stream_t stream, void *buf, int elem_bytes,
                 pad_size, unpad == 0, timeout_ns, stall_block);
 }
 
+// Failure-detection hook: the resident form of 0100(A, a, B, b) with its
+// grid barrier waiting for one arrival more than there are CTAs, bounded by
+// timeout_ns.  Must return true (error) with a timeout message, leave the
+// buffer as it was (no CTA writes) and the context usable.
+bool lm_debug_resident_stall(lm_stream_t stream, void *buf, int elem_bytes,
+                             int A, int a, int B, int b,
+                             unsigned long long timeout_ns) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!valid_e(elem_bytes))
+    return fail("element size must be 1, 2, 4 or 8 (got %d)", elem_bytes);
+  if (A <= 0 || a <= 1 || B <= 1 || b <= 0) return fail("dimensions must be positive");
+  if (buf == nullptr) return fail("null buffer");
+  if (misaligned(buf, elem_bytes))
+    return fail("buffer must be aligned to the element size");
+  uint32_t *status = device_status_word();
+  if (!status) return fail("resident: no status word");
+  const cudaError_t err =
+      launch_resident0100(s, buf, elem_bytes, (uint64_t)A, (uint64_t)a,
+                          (uint64_t)B, (uint64_t)b, status, timeout_ns, 1);
+  if (err == cudaErrorNotSupported)
+    return fail("resident: the shape does not fit shared memory");
+  if (err != cudaSuccess) return cuda_fail(err, "resident launch");
+  return check_status(s, "resident");
+}
+
 // Waits for `stream` and returns (then clears) the accumulated status of
 // waiting kernels on the current device: 0 = ok.
 unsigned lm_device_status(lm_stream_t stream) {

@@ -2310,7 +2310,8 @@ bool resident0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
 
 cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
                                 uint64_t a, uint64_t B, uint64_t b,
-                                uint32_t *status, uint64_t timeout_ns) {
+                                uint32_t *status, uint64_t timeout_ns,
+                                uint32_t missing) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaError_t err = cudaStreamIsCapturing(s, &cs);
   if (err != cudaSuccess) return err;
@@ -2329,7 +2330,7 @@ cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
     std::lock_guard<std::mutex> lock(g_res_mu);
     g.slot = d->next++ % kResSlots;
     d->arrivals[g.slot] += grid;
-    g.target = d->arrivals[g.slot];
+    g.target = d->arrivals[g.slot] + missing;
   }
   void *args[] = {&g};
   ProfScope ps(s, "resident");

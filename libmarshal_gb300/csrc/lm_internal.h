@@ -187,12 +187,15 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
 // staged form's blocks loaded by every CTA, a grid barrier, then written
 // transposed over the buffer: one cooperative launch, 2 x payload.
 // cudaErrorNotSupported when the shape does not fit or the stream is being
-// captured.  A barrier wait that runs out sets `status` and skips the writes.
+// captured.  A barrier wait that runs out sets `status` and skips the writes
+// (`missing` > 0, a failure-detection test: the barrier waits for that many
+// arrivals more than there are CTAs).
 bool resident0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
                           int e);
 cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
                                 uint64_t a, uint64_t B, uint64_t b,
-                                uint32_t *status, uint64_t timeout_ns);
+                                uint32_t *status, uint64_t timeout_ns,
+                                uint32_t missing = 0);
 
 // A 0100 moves whole units of b elements, so the same byte permutation is a
 // 0100 over elements of any width w dividing the unit's b*e bytes.  Widens

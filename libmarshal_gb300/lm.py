@@ -54,6 +54,8 @@ _SIGS = {
     "lm_bs_feasible": (_I, [_LL, _I, _I, _I, _I]),
     "lm_debug_pad_stall": (_B, [_VP, _VP, _I, _I, _I, _I, _I, _LL,
                                 ctypes.c_ulonglong]),
+    "lm_debug_resident_stall": (_B, [_VP, _VP, _I, _I, _I, _I, _I,
+                                     ctypes.c_ulonglong]),
     "lm_batch_create": (_B, [_VP]),
     "lm_batch_destroy": (None, [_VP]),
     "lm_batch_run": (_B, [_VP, _VP, _VP, _I, ctypes.c_uint]),

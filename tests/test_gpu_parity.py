@@ -649,3 +649,69 @@ def test_resident_form_is_the_route_for_7200x1800(L):
         assert list(ran) == ["resident"], ran
         assert ran["resident"][0] == 1
         assert np.array_equal(from_dev(d, e), O.t100(src, 7200, 1800, 1))
+
+
+def test_resident_barrier_timeout_is_reported(L, cuda):
+    """Failure detection for the resident form's grid barrier: a launch whose
+    barrier waits for one CTA more than it has gives up after 50 ms in every
+    CTA, reports the timeout, writes nothing, and the context stays
+    usable."""
+    import torch
+    A, a, B, b, e = 1, 3000, 1000, 1, 1
+    src = O.random_bits(a * B, e, 21)
+    d = to_dev(src)
+    keep = d.clone()
+    failed = L.lib().lm_debug_resident_stall(None, d.data_ptr(), e, A, a, B,
+                                             b, 50_000_000)
+    assert failed is True
+    assert "timed out" in L.last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(d, keep)
+    assert L.lib().lm_device_status(None) == 0
+    # the next resident launches (and their barrier slots) work
+    for _ in range(3):
+        L.transpose_0100(d, A, a, B, b, method=7, elem_bytes=e)
+        L.transpose_0100(d, A, B, a, b, method=7, elem_bytes=e)
+    assert np.array_equal(from_dev(d, e), src)
+
+
+def test_resident_concurrent_streams(L, cuda):
+    """Resident launches from several host threads on their own streams at
+    once: each launch gets its own barrier slot and target, so concurrent
+    launches (which may share the SMs) never pass each other's barrier;
+    every result bit-exact."""
+    import threading
+    import torch
+    shapes = [(1, 2000, 1500, 1, 1), (1, 1200, 900, 1, 2), (3, 400, 500, 1, 4),
+              (1, 777, 1333, 1, 8)]
+    errors = []
+
+    def work(k):
+        try:
+            T, a, B, b, e = shapes[k % len(shapes)]
+            s = torch.cuda.Stream()
+            src = O.random_bits(T * a * B * b, e, 100 + k)
+            d = to_dev(src)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(s):
+                for _ in range(5):
+                    L.transpose_0100(d, T, a, B, b, method=7, elem_bytes=e,
+                                     stream=s)
+                    L.transpose_0100(d, T, B, a, b, method=7, elem_bytes=e,
+                                     stream=s)
+                L.transpose_0100(d, T, a, B, b, method=7, elem_bytes=e,
+                                 stream=s)
+            s.synchronize()
+            got = d.cpu().numpy().view(O.DTYPES[e])
+            if not np.array_equal(got, O.t0100(src, T, a, B, b)):
+                errors.append(k)
+        except Exception as exc:  # reported below
+            errors.append((k, repr(exc)))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    assert L.lib().lm_device_status(None) == 0
