@@ -349,9 +349,19 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
     // (the 16-byte tile kernel sizes its own chunks to the GPU)
     const bool t010 = b == 1 && p.feasible && p.cluster == 1 &&
                       tile010_applies(buf, e, T, a, B);
-    const bool thin = m == Method::Auto && !t010 &&
-                      T * a * B * b * (uint64_t)e >= (1ull << 20) &&
-                      chunks * (uint64_t)p.cluster < (uint64_t)device_info().sms;
+    const uint64_t bytes = T * a * B * b * (uint64_t)e;
+    const uint64_t ctas = chunks * (uint64_t)p.cluster;
+    const uint64_t sms = (uint64_t)device_info().sms;
+    bool thin = m == Method::Auto && !t010 && bytes >= (1ull << 20) &&
+                ctas < sms;
+    // payloads the resident form takes (from 512 KB): the on-chip plan wins
+    // from half the SMs up (64 tiles of 64 x 4096 bytes in 2-CTA clusters:
+    // 0.0173 vs 0.0182 ms), the resident form below (one 1000 x 1000 byte
+    // tile over a 16-CTA cluster: 0.0336 vs 0.0144 ms)
+    if (m == Method::Auto && !t010 && p.feasible && bytes >= (512ull << 10) &&
+        !planner_beside_other_work() && !getenv("LM_NO_RESIDENT") &&
+        resident0100_applies(T, a, B, b, e))
+      thin = ctas * 2 < sms;
     if (p.feasible && !thin)
       return check_launch(launch_bs0100(s, buf, e, T, (uint32_t)a,
                                         (uint32_t)B, (uint32_t)b, p),
