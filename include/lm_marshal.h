@@ -30,7 +30,9 @@
  *         (421 MB for 16384 x 12289 fp32), plus 8 bytes per row;
  *       the staged form (blocks transposed out of place, then copied back):
  *         the payload's size plus 16 bytes;
- *       padding: 8 bytes per 4096-element task.
+ *       padding: 8 bytes per 4096-element task;
+ *     payloads that fit the shared memory of all SMs (about 30 MB on GB300)
+ *     move through shared memory instead and take no scratch.
  *     When the pool cannot supply the stash or the staged form's scratch
  *     the planner falls through to a method that needs less (ultimately
  *     cycle following); lm_transpose_100_noalloc allocates nothing.
