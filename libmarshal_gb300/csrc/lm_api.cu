@@ -360,8 +360,13 @@ static bool do_0100(cudaStream_t s, void *buf, int e, uint64_t T, uint64_t a,
     // tile over a 16-CTA cluster: 0.0336 vs 0.0144 ms)
     if (m == Method::Auto && !t010 && p.feasible && bytes >= (512ull << 10) &&
         !planner_beside_other_work() && !getenv("LM_NO_RESIDENT") &&
-        resident0100_applies(T, a, B, b, e))
-      thin = ctas * 2 < sms;
+        resident0100_applies(T, a, B, b, e)) {
+      // (under stream capture the resident form does not run)
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(s, &cs) == cudaSuccess &&
+          cs == cudaStreamCaptureStatusNone)
+        thin = ctas * 2 < sms;
+    }
     if (p.feasible && !thin)
       return check_launch(launch_bs0100(s, buf, e, T, (uint32_t)a,
                                         (uint32_t)B, (uint32_t)b, p),
