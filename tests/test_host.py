@@ -59,6 +59,14 @@ def test_library_reports_errors_without_a_gpu_call(built):
     assert "aligned" in lm.last_error()
     assert L.lm_padding(None, 0x1001, 2, 3, 4, 5, None) is True
     assert "aligned" in lm.last_error()
+    # method codes 0..7 (7: held in shared memory); others refused
+    assert L.lm_transpose_0100_method(None, 0x1000, 4, 1, 4, 5, 1, 8,
+                                      None) is True
+    assert "0..7" in lm.last_error()
+    assert L.lm_debug_resident_stall(None, 0x1002, 4, 1, 4, 5, 1, 1000) is True
+    assert "aligned" in lm.last_error()
+    assert L.lm_debug_resident_stall(None, 0x1000, 4, 1, 1, 5, 1, 1000) is True
+    assert "dimensions" in lm.last_error()
 
 
 def _fastdiv(d):
