@@ -715,3 +715,19 @@ def test_resident_concurrent_streams(L, cuda):
         t.join()
     assert not errors, errors
     assert L.lib().lm_device_status(None) == 0
+
+
+@pytest.mark.parametrize("e", [1, 4])
+def test_staged_l2_copy_back_sizes(L, e):
+    """The staged form's copy back by cudaMemcpyAsync (up to 48 MB and from
+    208 MB) and by the kernel that drops each scratch line from L2 once read
+    (48-208 MB): one transposition on each side of the lower edge and one
+    inside the range, bit-exact against the oracle."""
+    for (A, B) in ((4000, 10000 // e), (4000, 16000 // e), (6000, 16000 // e)):
+        src = O.random_bits(A * B, e, A + B)
+        d = to_dev(src)
+        L.transpose_0100(d, 1, A, B, 1, method=6, elem_bytes=e)
+        assert np.array_equal(from_dev(d, e), O.t0100(src, 1, A, B, 1)), \
+            (A, B, e)
+        del d
+    assert L.lib().lm_device_status(None) == 0
