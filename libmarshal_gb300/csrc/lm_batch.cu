@@ -1103,11 +1103,12 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
 
 // Persistent: every CTA walks blocks (claimed item by item from the work
 // counter) with two shared-memory stages, loading block n+1 by bulk copies
-// while it writes block n.
+// (issued by all warps) while it writes block n.
 // MB: CTAs per SM the registers are sized for.  Three suit the mixed
-// batches and 1-byte blocks; the vectorized store of 2-byte blocks wants the
-// registers of two (16384 x 16384 2-byte staged transposition: gather 0.358
-// vs 0.436 ms, while 1-byte blocks lose 0.236 -> 0.289 ms).
+// batches and 1-byte blocks; the vectorized store of 2-byte blocks wanted
+// the registers of two when it was first measured (16384 x 16384 2-byte
+// staged transposition: gather 0.358 vs 0.436 ms, while 1-byte blocks lost
+// 0.236 -> 0.289 ms).
 template <int MB>
 __global__ void __launch_bounds__(kStageThreads, MB) k_batch_gather(BatchArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];

@@ -241,10 +241,11 @@ __global__ void __launch_bounds__(kSaveThreads) k_stash_save(StashArgs g) {
 }
 
 // K2: the wavefront, warp-specialised.  Per CTA:
-//   warps 0-3 (producers): gather step J into ring stage J % kStages (warp 0
-//     issues one bulk copy per row of a 16-byte aligned superset of its
-//     strip, rowoff[] records where the strip starts; or, with cp.async, all
-//     four warps copy 16-byte pieces); completion lands on `full`;
+//   warps 0-3 (producers): gather step J into ring stage J % kStages (one
+//     bulk copy per row of a 16-byte aligned superset of its strip, each
+//     issued by the producer thread that owns the row, rowoff[] records
+//     where the strip starts; or, with cp.async, all four warps copy
+//     16-byte pieces); completion lands on `full`;
 //   warp 4 (publisher): when stage J has landed, publishes progress = J+1;
 //   warp 5 (checker): waits for the CTAs whose rows hold original data in
 //     step J's destination range, then marks the stage `ready`;
