@@ -1105,10 +1105,10 @@ __device__ void gather_store(const BJob &j, uint32_t q, const unsigned char *buf
 // counter) with two shared-memory stages, loading block n+1 by bulk copies
 // (issued by all warps) while it writes block n.
 // MB: CTAs per SM the registers are sized for.  Three suit the mixed
-// batches and 1-byte blocks; the vectorized store of 2-byte blocks wanted
-// the registers of two when it was first measured (16384 x 16384 2-byte
-// staged transposition: gather 0.358 vs 0.436 ms, while 1-byte blocks lost
-// 0.236 -> 0.289 ms).
+// batches and 1-, 4- and 8-byte blocks; 2-byte blocks run 0-3 % faster with
+// the registers of two (staged 100s of 2-byte elements, 4096 x 32768:
+// gather 0.0933 vs 0.0963 ms; 500 x 268435: 0.161 vs 0.167 ms; 1-byte
+// 16384 x 16384 the other way: 0.126 vs 0.121 ms).
 template <int MB>
 __global__ void __launch_bounds__(kStageThreads, MB) k_batch_gather(BatchArgs g) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -2077,7 +2077,7 @@ cudaError_t launch_staged0100(cudaStream_t s, void *buf, int e, uint64_t T,
   size_t stage = 0;
   if (!staged_job(g.single, jb, nz, &nblk, &stage)) return cudaErrorInvalidValue;
   g.single.scratch = reinterpret_cast<char *>(scratch);
-  auto gather = (e == 2 && g.single.vb1) ? k_batch_gather<2> : k_batch_gather<3>;
+  auto gather = e == 2 ? k_batch_gather<2> : k_batch_gather<3>;
   const size_t dyn = 2 * stage;
   cudaError_t err = cudaSuccess;
   if (dyn > 48 * 1024 &&
