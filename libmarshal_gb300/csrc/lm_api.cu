@@ -707,7 +707,7 @@ static bool do_transpose(cudaStream_t s, void *buf, int e, int64_t A,
   // Every stage code yields the same final layout, the full transpose
   // [A*a][B*b] -> [B*b][A*a]: with the 010 variant left to the library it
   // runs as one planned 100, which moves 2-4 x payload where the staged
-  // sequences move 2 x payload per stage (7200 x 1800: 2.4-6.5 x faster,
+  // sequences move 2 x payload per stage (7200 x 1800: 2.4-7.7 x faster,
   // int8 and fp16 in one launch held in shared memory).  Forced variants run
   // the reference's stages.
   if (variant010 == 0) return t100(A * a, B * b, 1);

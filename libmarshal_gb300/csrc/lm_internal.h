@@ -80,6 +80,9 @@ int prepare_launch(const void *kern, LaunchCache &c, size_t smem, int threads,
 struct TuneParams {
   uint32_t staged_block_bytes = 0;  // staged form: bytes staged per block
   int stash_per_sm = 0;             // stash plan: CTAs per SM (1 or 2)
+  // staged form: square blocks of S x S units get S * staged_wide columns
+  // (0 or 1: square)
+  uint32_t staged_wide = 0;
 };
 TuneParams &tune_params();
 
