@@ -2295,6 +2295,53 @@ bool plan_resident(ResArgs &g, uint32_t *grid, size_t *dyn, void *buf,
   return ok;
 }
 
+// plan_resident with the last 16 plans of this thread kept (keyed by shape,
+// element size, device and the buffer's address modulo 16, which decides
+// the vector stores): the planner asks whether the resident form applies
+// and then launches it, and small conversions are called again and again.
+bool plan_resident_cached(ResArgs &g, uint32_t *grid, size_t *dyn, void *buf,
+                          uint64_t T, uint64_t a, uint64_t B, uint64_t b,
+                          int e, size_t max_dyn) {
+  struct Entry {
+    uint64_t T = 0, a = 0, B = 0, b = 0;
+    size_t max_dyn = 0;
+    int e = 0, dev = -1;
+    uint32_t mis = 0;
+    bool used = false, ok = false;
+    ResArgs g{};
+    uint32_t grid = 0;
+    size_t dyn = 0;
+  };
+  static thread_local Entry cache[16];
+  static thread_local uint32_t next = 0;
+  const int dev = device_info().device;
+  const uint32_t mis = (uint32_t)((uintptr_t)buf & 15);
+  for (const Entry &c : cache) {
+    if (!c.used || c.T != T || c.a != a || c.B != B || c.b != b || c.e != e ||
+        c.dev != dev || c.mis != mis || c.max_dyn != max_dyn)
+      continue;
+    if (c.ok) {
+      g = c.g;
+      g.job.base = reinterpret_cast<char *>(buf);
+      *grid = c.grid;
+      *dyn = c.dyn;
+    }
+    return c.ok;
+  }
+  Entry &c = cache[next++ % 16];
+  c = Entry();
+  c.T = T, c.a = a, c.B = B, c.b = b, c.e = e, c.dev = dev, c.mis = mis;
+  c.max_dyn = max_dyn;
+  c.used = true;
+  c.ok = plan_resident(c.g, &c.grid, &c.dyn, buf, T, a, B, b, e, max_dyn);
+  if (c.ok) {
+    g = c.g;
+    *grid = c.grid;
+    *dyn = c.dyn;
+  }
+  return c.ok;
+}
+
 // The device's ResDevice, set up on first use (nullptr on failure).
 ResDevice *res_device() {
   const DeviceInfo &di = device_info();
@@ -2328,7 +2375,8 @@ bool resident0100_applies(uint64_t T, uint64_t a, uint64_t B, uint64_t b,
   ResArgs g{};
   uint32_t grid = 0;
   size_t dyn = 0;
-  return plan_resident(g, &grid, &dyn, nullptr, T, a, B, b, e, d->max_dyn);
+  return plan_resident_cached(g, &grid, &dyn, nullptr, T, a, B, b, e,
+                              d->max_dyn);
 }
 
 cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
@@ -2344,7 +2392,7 @@ cudaError_t launch_resident0100(cudaStream_t s, void *buf, int e, uint64_t T,
   ResArgs g{};
   uint32_t grid = 0;
   size_t dyn = 0;
-  if (!plan_resident(g, &grid, &dyn, buf, T, a, B, b, e, d->max_dyn))
+  if (!plan_resident_cached(g, &grid, &dyn, buf, T, a, B, b, e, d->max_dyn))
     return cudaErrorNotSupported;
   g.job.scratch = g.job.base;
   g.status = status;
