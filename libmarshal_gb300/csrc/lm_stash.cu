@@ -579,7 +579,48 @@ static int wave_occupancy_e(int e, size_t smem) {
   }
 }
 
+static StashPlan plan_stash_uncached(uint64_t A, uint64_t B, uint32_t b,
+                                     int e);
+
+// plan_stash with the last 16 plans of this thread kept: a plan sums every
+// row's stash slot (two 64-bit divisions per row), and the planner, the
+// batch router and the tuner ask for the same shapes again and again.  The
+// key holds everything the plan reads: the shape, the device, the tuned
+// CTAs per SM and the LM_STASH_* overrides.
 StashPlan plan_stash(uint64_t A, uint64_t B, uint32_t b, int e) {
+  struct Entry {
+    uint64_t A = 0, B = 0;
+    uint32_t b = 0;
+    int e = 0, dev = -1, tuned = 0;
+    long long strip = 0, per_sm = 0, margin = 0;
+    bool used = false;
+    StashPlan p;
+  };
+  static thread_local Entry cache[16];
+  static thread_local uint32_t next = 0;
+  const char *es = getenv("LM_STASH_STRIP");
+  const char *ep = getenv("LM_STASH_PER_SM");
+  const char *em = getenv("LM_STASH_MARGIN");
+  Entry k;
+  k.A = A, k.B = B, k.b = b, k.e = e;
+  k.dev = device_info().device;
+  k.tuned = tune_params().stash_per_sm;
+  k.strip = es ? atoll(es) : 0;
+  k.per_sm = ep ? atoll(ep) : 0;
+  k.margin = em ? atoll(em) : 0;
+  for (const Entry &c : cache)
+    if (c.used && c.A == k.A && c.B == k.B && c.b == k.b && c.e == k.e &&
+        c.dev == k.dev && c.tuned == k.tuned && c.strip == k.strip &&
+        c.per_sm == k.per_sm && c.margin == k.margin)
+      return c.p;
+  k.used = true;
+  k.p = plan_stash_uncached(A, B, b, e);
+  cache[next++ % 16] = k;
+  return k.p;
+}
+
+static StashPlan plan_stash_uncached(uint64_t A, uint64_t B, uint32_t b,
+                                     int e) {
   StashPlan p;
   if (e != 1 && e != 2 && e != 4 && e != 8) return p;
   if (A < 2 || B < 2 || b == 0) return p;
